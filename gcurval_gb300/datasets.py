@@ -1,0 +1,303 @@
+"""Seeded synthetic curve batches (the five workloads the library is measured on).
+
+The reference ships no benchmark inputs besides its text B-spline bundle; these
+generators produce curves with the shapes, sizes and value distributions of the
+five measured workloads, from ``numpy.random.default_rng(seed)``:
+
+* ``ellipses``          4,096 2D ellipses, a, b ~ U[0.1, 10], rotation
+                        ~ U[0, 2 pi), centre ~ U[-100, 100]^2, one interval
+                        t in [0, 2 pi]; 1,000 uniformly spaced samples.
+* ``uniform_bsplines``  10,000 clamped uniform cubic 2D B-splines, 64 control
+                        points as a random walk with N(0, 1) steps per axis
+                        (61 knot intervals); 1,024 samples.
+* ``mixed3d_bsplines``  100,000 clamped 3D B-splines, degree 3 or 5, 32-256
+                        control points, interior knots sorted U[0, 1] draws,
+                        N(0, 0.5) random-walk steps; 2,048 samples.
+* ``uneven_batch``      1,000,000 curves: 20 % ellipses, 80 % 2D/3D B-splines of
+                        degree 2-5 with log-uniform 4-4,096 control points and 5 %
+                        near-duplicate interior knots (gap 1e-6); log-uniform
+                        16-8,192 samples per curve.
+
+The batch layout is the one the C ABI takes (``gcv_create_batch`` in
+include/gcurval_gb300.h): per-curve kind / degree / dim, CSR offsets into one
+knot array and one control array.  Ellipses store ``a, b, rotation, cx, cy`` as
+their control data and the knot vector ``{0, 2 pi}``.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+KIND_ELLIPSE = 0
+KIND_BSPLINE = 1
+TWO_PI = 2.0 * math.pi
+
+
+@dataclasses.dataclass
+class CurveBatch:
+    kind: np.ndarray  # uint8[n]
+    degree: np.ndarray  # uint8[n]
+    dim: np.ndarray  # uint8[n]
+    knot_off: np.ndarray  # int64[n + 1]
+    knots: np.ndarray  # float64
+    ctrl_off: np.ndarray  # int64[n + 1] (in doubles)
+    ctrl: np.ndarray  # float64
+    n_samples: np.ndarray  # int32[n]
+    positions: np.ndarray | None = None  # float64[sum(n_samples)], relative
+    name: str = ""
+    rtol: float = 1e-10
+
+    @property
+    def n_curve(self) -> int:
+        return int(self.kind.shape[0])
+
+    @property
+    def n_segments(self) -> np.ndarray:
+        nk = np.diff(self.knot_off)
+        p = self.degree.astype(np.int64)
+        return np.where(self.kind == KIND_ELLIPSE, nk - 1, nk - 2 * p - 1)
+
+    @property
+    def total_samples(self) -> int:
+        return int(self.n_samples.astype(np.int64).sum())
+
+    def sample_positions(self) -> np.ndarray:
+        """Uniformly spaced relative positions j / (n - 1) for every curve."""
+        if self.positions is None:
+            self.positions = uniform_positions(self.n_samples)
+        return self.positions
+
+    def subset(self, idx) -> "CurveBatch":
+        """A new batch holding curves ``idx`` (in that order)."""
+        idx = np.asarray(idx, dtype=np.int64)
+        kl = np.diff(self.knot_off)[idx]
+        cl = np.diff(self.ctrl_off)[idx]
+        ko = np.concatenate([[0], np.cumsum(kl)]).astype(np.int64)
+        co = np.concatenate([[0], np.cumsum(cl)]).astype(np.int64)
+        knots = np.concatenate([self.knots[self.knot_off[i]:self.knot_off[i + 1]] for i in idx]) if len(idx) else np.zeros(0)
+        ctrl = np.concatenate([self.ctrl[self.ctrl_off[i]:self.ctrl_off[i + 1]] for i in idx]) if len(idx) else np.zeros(0)
+        ns = self.n_samples[idx].copy()
+        pos = None
+        if self.positions is not None:
+            so = np.concatenate([[0], np.cumsum(self.n_samples.astype(np.int64))])
+            pos = np.concatenate([self.positions[so[i]:so[i + 1]] for i in idx]) if len(idx) else np.zeros(0)
+        return CurveBatch(self.kind[idx].copy(), self.degree[idx].copy(), self.dim[idx].copy(), ko,
+                          np.ascontiguousarray(knots, dtype=np.float64), co,
+                          np.ascontiguousarray(ctrl, dtype=np.float64), ns, pos, self.name, self.rtol)
+
+    def nbytes(self) -> int:
+        return sum(a.nbytes for a in (self.kind, self.degree, self.dim, self.knot_off, self.knots,
+                                      self.ctrl_off, self.ctrl))
+
+
+def uniform_positions(n_samples: np.ndarray) -> np.ndarray:
+    """Relative positions j / (n - 1), j = 0..n-1, for each curve (0 when n == 1)."""
+    n_samples = np.asarray(n_samples, dtype=np.int64)
+    total = int(n_samples.sum())
+    off = np.concatenate([[0], np.cumsum(n_samples)])
+    j = np.arange(total, dtype=np.int64) - np.repeat(off[:-1], n_samples)
+    den = np.repeat(np.maximum(n_samples - 1, 1), n_samples).astype(np.float64)
+    return j.astype(np.float64) / den
+
+
+def _pack(kind, degree, dim, knot_lists_len, knots, ctrl_len, ctrl, n_samples, name, rtol):
+    knot_off = np.concatenate([[0], np.cumsum(knot_lists_len)]).astype(np.int64)
+    ctrl_off = np.concatenate([[0], np.cumsum(ctrl_len)]).astype(np.int64)
+    return CurveBatch(np.asarray(kind, np.uint8), np.asarray(degree, np.uint8), np.asarray(dim, np.uint8),
+                      knot_off, np.ascontiguousarray(knots, np.float64), ctrl_off,
+                      np.ascontiguousarray(ctrl, np.float64), np.asarray(n_samples, np.int32), None, name, rtol)
+
+
+def _ellipse_params(rng, n):
+    a = rng.uniform(0.1, 10.0, n)
+    b = rng.uniform(0.1, 10.0, n)
+    rot = rng.uniform(0.0, TWO_PI, n)
+    cx = rng.uniform(-100.0, 100.0, n)
+    cy = rng.uniform(-100.0, 100.0, n)
+    return np.stack([a, b, rot, cx, cy], axis=1)
+
+
+def ellipses(n: int = 4096, n_samples: int = 1000, seed: int = 0, rtol: float = 1e-10) -> CurveBatch:
+    rng = np.random.default_rng(seed)
+    prm = _ellipse_params(rng, n)
+    knots = np.tile(np.array([0.0, TWO_PI]), n)
+    return _pack(np.zeros(n), np.zeros(n), np.full(n, 2), np.full(n, 2), knots, np.full(n, 5),
+                 prm.reshape(-1), np.full(n, n_samples), "ellipses", rtol)
+
+
+def ellipses_from_axes(a, b, rot=None, cx=None, cy=None, n_samples=0) -> CurveBatch:
+    a = np.asarray(a, np.float64)
+    n = a.shape[0]
+    z = np.zeros(n)
+    prm = np.stack([a, np.asarray(b, np.float64), z if rot is None else np.asarray(rot, np.float64),
+                    z if cx is None else np.asarray(cx, np.float64), z if cy is None else np.asarray(cy, np.float64)], 1)
+    return _pack(np.zeros(n), np.zeros(n), np.full(n, 2), np.full(n, 2), np.tile([0.0, TWO_PI], n),
+                 np.full(n, 5), prm.reshape(-1), np.full(n, n_samples), "ellipses", 1e-10)
+
+
+def clamped_uniform_knots(n_ctrl: int, degree: int) -> np.ndarray:
+    n_int = n_ctrl - degree - 1
+    inner = np.arange(1, n_int + 1, dtype=np.float64) / (n_int + 1)
+    return np.concatenate([np.zeros(degree + 1), inner, np.ones(degree + 1)])
+
+
+def uniform_bsplines(n: int = 10000, n_ctrl: int = 64, degree: int = 3, dim: int = 2, n_samples: int = 1024,
+                     seed: int = 0, step_sigma: float = 1.0, rtol: float = 1e-10) -> CurveBatch:
+    rng = np.random.default_rng(seed)
+    steps = rng.normal(0.0, step_sigma, size=(n, n_ctrl - 1, dim))
+    pts = np.concatenate([np.zeros((n, 1, dim)), np.cumsum(steps, axis=1)], axis=1)
+    kv = clamped_uniform_knots(n_ctrl, degree)
+    knots = np.tile(kv, n)
+    return _pack(np.ones(n), np.full(n, degree), np.full(n, dim), np.full(n, kv.size), knots,
+                 np.full(n, n_ctrl * dim), pts.reshape(-1), np.full(n, n_samples), "uniform_bsplines", rtol)
+
+
+def _segmented_sorted_uniform(rng, counts: np.ndarray) -> np.ndarray:
+    """For each count m, m sorted U(0,1) draws (via normalised exponential spacings), flat."""
+    counts = np.asarray(counts, np.int64)
+    tot = int((counts + 1).sum())
+    e = rng.exponential(1.0, tot)
+    seg = np.repeat(np.arange(counts.size), counts + 1)
+    cs = np.cumsum(e)
+    starts = np.concatenate([[0], np.cumsum(counts + 1)])
+    base = np.concatenate([[0.0], cs])[starts[:-1]]
+    local = cs - base[seg]
+    total = local[starts[1:] - 1]
+    val = local / total[seg]
+    keep = np.ones(tot, bool)
+    keep[starts[1:] - 1] = False  # drop the last (== 1) of each group
+    return val[keep]
+
+
+def _random_knot_bsplines(rng, degree, dim, n_ctrl, step_sigma, dup_frac=0.0, dup_gap=1e-6):
+    """Clamped B-splines with sorted-uniform interior knots; per-curve degree/dim/n_ctrl arrays."""
+    n = degree.size
+    n_int = n_ctrl - degree - 1
+    inner = _segmented_sorted_uniform(rng, n_int)
+    if dup_frac > 0.0 and inner.size:
+        # 5 % of interior knots become previous + gap (near-duplicate knots)
+        io = np.concatenate([[0], np.cumsum(n_int)])
+        first = np.zeros(inner.size, bool)
+        first[io[:-1][n_int > 0]] = True
+        pick = (rng.random(inner.size) < dup_frac) & ~first
+        idx = np.nonzero(pick)[0]
+        inner[idx] = np.minimum(inner[idx - 1] + dup_gap, 1.0)
+        # keep each curve's interior sorted after the replacements
+        order = np.lexsort((inner, np.repeat(np.arange(n), n_int)))
+        inner = inner[order]
+    n_knots = n_ctrl + degree + 1
+    total_k = int(n_knots.sum())
+    knots = np.empty(total_k)
+    ko = np.concatenate([[0], np.cumsum(n_knots)])
+    io = np.concatenate([[0], np.cumsum(n_int)])
+    # vectorised fill: position within curve
+    cid = np.repeat(np.arange(n), n_knots)
+    j = np.arange(total_k) - ko[cid]
+    p = degree[cid]
+    lo = j <= p
+    hi = j >= (n_ctrl[cid])
+    mid = ~(lo | hi)
+    knots[lo] = 0.0
+    knots[hi] = 1.0
+    knots[mid] = inner[io[cid[mid]] + (j[mid] - p[mid] - 1)]
+    # control points: random walk per curve, dim per curve
+    clen = n_ctrl * dim
+    tot_c = int(clen.sum())
+    steps = rng.normal(0.0, step_sigma, tot_c)
+    co = np.concatenate([[0], np.cumsum(clen)])
+    # zero the first point of each curve, cumulative sum per (curve, axis)
+    ccid = np.repeat(np.arange(n), clen)
+    k = np.arange(tot_c) - co[ccid]
+    d = dim[ccid].astype(np.int64)
+    axis = k % d
+    first = k < d
+    steps[first] = 0.0
+    # segmented cumsum along each (curve, axis) stream: reorder to axis-major within curve
+    key = ccid * 3 + axis
+    order = np.lexsort((k, key))
+    s = steps[order]
+    cs = np.cumsum(s)
+    keys_sorted = key[order]
+    starts = np.r_[0, np.nonzero(np.diff(keys_sorted))[0] + 1]
+    grp = np.repeat(np.arange(starts.size), np.diff(np.r_[starts, s.size]))
+    offs = np.r_[0.0, cs][starts][grp]
+    ctrl = np.empty(tot_c)
+    ctrl[order] = cs - offs
+    return n_knots, knots, clen, ctrl
+
+
+def mixed3d_bsplines(n: int = 100_000, n_samples: int = 2048, seed: int = 0, rtol: float = 1e-8) -> CurveBatch:
+    rng = np.random.default_rng(seed)
+    degree = np.where(rng.random(n) < 0.5, 3, 5).astype(np.int64)
+    n_ctrl = rng.integers(32, 257, n).astype(np.int64)
+    dim = np.full(n, 3, np.int64)
+    n_knots, knots, clen, ctrl = _random_knot_bsplines(rng, degree, dim, n_ctrl, 0.5)
+    return _pack(np.ones(n), degree, dim, n_knots, knots, clen, ctrl, np.full(n, n_samples),
+                 "mixed3d_bsplines", rtol)
+
+
+def _log_uniform_int(rng, lo, hi, n):
+    return np.floor(np.exp(rng.uniform(math.log(lo), math.log(hi + 1), n))).astype(np.int64).clip(lo, hi)
+
+
+def uneven_batch(n: int = 1_000_000, seed: int = 0, rtol: float = 1e-8,
+                 max_ctrl: int = 4096, min_samples: int = 16, max_samples: int = 8192) -> CurveBatch:
+    rng = np.random.default_rng(seed)
+    is_ell = rng.random(n) < 0.2
+    ne = int(is_ell.sum())
+    nb = n - ne
+    degree = rng.integers(2, 6, nb).astype(np.int64)
+    dim = rng.integers(2, 4, nb).astype(np.int64)
+    n_ctrl = np.maximum(_log_uniform_int(rng, 4, max_ctrl, nb), degree + 1)
+    n_knots_b, knots_b, clen_b, ctrl_b = _random_knot_bsplines(rng, degree, dim, n_ctrl, 1.0, dup_frac=0.05)
+    prm = _ellipse_params(rng, ne)
+    n_samp = _log_uniform_int(rng, min_samples, max_samples, n)
+    # interleave ellipses and B-splines in curve order
+    kind = np.where(is_ell, KIND_ELLIPSE, KIND_BSPLINE)
+    deg = np.zeros(n, np.int64)
+    dm = np.full(n, 2, np.int64)
+    deg[~is_ell] = degree
+    dm[~is_ell] = dim
+    klen = np.full(n, 2, np.int64)
+    klen[~is_ell] = n_knots_b
+    clen = np.full(n, 5, np.int64)
+    clen[~is_ell] = clen_b
+    ko = np.concatenate([[0], np.cumsum(klen)])
+    co = np.concatenate([[0], np.cumsum(clen)])
+    knots = np.empty(int(ko[-1]))
+    ctrl = np.empty(int(co[-1]))
+    # ellipse parts
+    e_idx = np.nonzero(is_ell)[0]
+    knots[ko[e_idx]] = 0.0
+    knots[ko[e_idx] + 1] = TWO_PI
+    ctrl[(co[e_idx][:, None] + np.arange(5)).reshape(-1)] = prm.reshape(-1)
+    # B-spline parts (copy contiguous runs)
+    b_idx = np.nonzero(~is_ell)[0]
+    kb_off = np.concatenate([[0], np.cumsum(n_knots_b)])
+    cb_off = np.concatenate([[0], np.cumsum(clen_b)])
+    dst_k = np.repeat(ko[b_idx], n_knots_b) + (np.arange(kb_off[-1]) - np.repeat(kb_off[:-1], n_knots_b))
+    knots[dst_k] = knots_b
+    dst_c = np.repeat(co[b_idx], clen_b) + (np.arange(cb_off[-1]) - np.repeat(cb_off[:-1], clen_b))
+    ctrl[dst_c] = ctrl_b
+    return _pack(kind, deg, dm, klen, knots, clen, ctrl, n_samp, "uneven_batch", rtol)
+
+
+WORKLOADS = {
+    "ellipses": ellipses,
+    "uniform_bsplines": uniform_bsplines,
+    "mixed3d_bsplines": mixed3d_bsplines,
+    "uneven_batch": uneven_batch,
+}
+
+
+def reference_layout(batch: CurveBatch):
+    """(degree, dim, knots_offset int32[n+1], knots, ctrl) for a batch of B-splines that share
+    one degree and dimension: the layout of the reference's B-spline sample
+    (samples/sample2_bspline/arclength_calculate.h:505-518)."""
+    assert np.all(batch.kind == KIND_BSPLINE)
+    p = int(batch.degree[0])
+    d = int(batch.dim[0])
+    assert np.all(batch.degree == p) and np.all(batch.dim == d)
+    return p, d, batch.knot_off.astype(np.int32), batch.knots, batch.ctrl
