@@ -1,0 +1,380 @@
+"""Throughput of the arc-length path (table build + arc-length sampling) on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload uniform_bsplines|ellipses|mixed3d_bsplines|uneven_batch]
+                    [--precision plain|mixed]
+
+A step is one pass of the hot path over one batch: createArclengthTable plus
+arclengthReverse of every sample of every curve.  Prints ONE JSON line (rank 0).
+
+* ``value``  curves/s with the batch already resident in HBM (device-timed with
+             CUDA events around each step; L2 is flushed between steps).
+* ``e2e``    the same metric through the public API with host buffers: context
+             creation from host arrays (H2D), table, sampling into host memory
+             (H2D positions, D2H parameters), destroy; wall clock per step.
+* ``roofline`` for the dominant kernel, ``cpu_baseline`` (the reference's CPU
+             algorithm on a bounded sample, all host threads), ``clocks``.
+
+N > 1 (torchrun): every rank runs its own batch of the full size (weak
+scaling, independent curves, no collective on the data path); the step time
+is the max over ranks.  ``--impl reference`` times the reference's CPU
+implementation of the path on this host (rank 0 only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "curves/s & samples/s at rel err <=1e-8 vs FP64: learned+mixed vs plain, 1 GB300"
+
+WORKLOADS = {
+    # name: (generator kwargs, description)
+    "uniform_bsplines": (dict(n=10000, n_ctrl=64, degree=3, dim=2, n_samples=1024),
+                         "10,000 clamped uniform cubic 2D B-splines, 64 random-walk control points "
+                         "(61 knot intervals), 1,024 samples per curve"),
+    "ellipses": (dict(n=4096, n_samples=1000),
+                 "4,096 rotated/centred 2D ellipses, a,b~U[0.1,10], 1,000 samples per curve"),
+    "mixed3d_bsplines": (dict(n=100_000, n_samples=2048),
+                         "100,000 3D clamped B-splines, degree 3|5, 32-256 control points, 2,048 samples"),
+    "uneven_batch": (dict(n=1_000_000),
+                     "1,000,000 uneven curves (20% ellipses, 80% 2D/3D B-splines degree 2-5, 4-4,096 "
+                     "control points, 5% near-duplicate knots), 16-8,192 samples per curve"),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="uniform_bsplines")
+    ap.add_argument("--precision", choices=["plain", "mixed"], default="plain")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-sample-curves", type=int, default=0, help="curves in the CPU-baseline sample (0: auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def make_batch(workload: str, seed: int):
+    from gcurval_gb300 import datasets as ds
+    kw, _ = WORKLOADS[workload]
+    gen = ds.WORKLOADS[workload]
+    b = gen(seed=seed, **kw)
+    b.sample_positions()
+    return b
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------- CPU side
+def cpu_sample(batch, n_curves: int):
+    idx = np.linspace(0, batch.n_curve - 1, n_curves).astype(np.int64)
+    sub = batch.subset(np.unique(idx))
+    sub.sample_positions()
+    return sub
+
+
+def run_cpu_reference(sub, nthreads: int, prefer_reference: bool = True):
+    """One pass of the reference CPU algorithm over `sub`: (seconds, kind)."""
+    from oracle import oracle as orc
+    if prefer_reference and orc.reference_available():
+        try:
+            ref = orc.Reference(sub, nthreads=nthreads)
+            t0 = time.perf_counter()
+            ref.run(sub.n_samples, sub.positions, True, 0)
+            return time.perf_counter() - t0, "reference"
+        except ValueError:
+            pass  # mixed kinds: the reference driver takes one kind per batch
+    t0 = time.perf_counter()
+    o = orc.Oracle(sub, nthreads=nthreads)
+    o.reverse(sub.n_samples, sub.positions, True, 0)
+    return time.perf_counter() - t0, "port"
+
+
+def auto_cpu_curves(batch) -> int:
+    # about 10-20 s of single-thread CPU work, spread over the host threads
+    per_curve = 6e-3 * float(batch.n_segments.mean()) / 61.0 + 3.4e-6 * float(batch.n_samples.mean())
+    return int(max(16, min(batch.n_curve, 15.0 / max(per_curve, 1e-6))))
+
+
+# --------------------------------------------------------------- our arm
+def flops_per_eval(batch) -> float:
+    """FP64 flops of one |C'| evaluation (add/mul/sqrt/div 1, FMA 2), batch mean."""
+    p = batch.degree.astype(np.float64)
+    d = batch.dim.astype(np.float64)
+    bs = d * 2.0 * np.maximum(p - 1, 0) + (2.0 * d - 1.0) + 1.0  # Horner, squared norm, sqrt
+    ell = 1.0 + 2.0 + 2.0 + 1.0 + 20.0  # s^2, fma, sqrt, scale + sinpi (counted as 20)
+    return float(np.mean(np.where(batch.kind == 0, ell, bs)))
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    if args.impl == "reference":
+        if rank == 0:
+            reference_arm(args)
+        if dist:
+            dist.destroy_process_group()
+        return
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import gcurval_gb300 as g
+    from gcurval_gb300 import _lib
+
+    precision = g.GCV_MIXED if args.precision == "mixed" else g.GCV_PLAIN_FP64
+    batch = make_batch(args.workload, seed=rank)
+    pos = batch.positions
+    n_curves, n_samples = batch.n_curve, batch.total_samples
+
+    # ---- device-resident arm ------------------------------------------------
+    tk = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)
+    d_arr = (tk(batch.kind, torch.uint8), tk(batch.degree, torch.uint8), tk(batch.dim, torch.uint8),
+             tk(batch.knot_off, torch.int64), tk(batch.knots, torch.float64), tk(batch.ctrl_off, torch.int64),
+             tk(batch.ctrl, torch.float64))
+    d_cnt = tk(batch.n_samples, torch.int32)
+    d_pos = tk(pos, torch.float64)
+    d_out = torch.empty(n_samples, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    calc = g.ArclengthCalculateGpu.from_device_batch(*d_arr, precision=precision, collect_stats=True)
+
+    def step():
+        calc.createArclengthTable()
+        calc.arclengthReverseInto(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    st0 = calc.stats()
+    launches0 = st0["n_launches"]
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    ms_len, ms_samp, n_newton, n_panels = [], [], [], []
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            evs[i][0].record()
+            step()
+            evs[i][1].record()
+            s = calc.stats()  # synchronises; outside the events
+            ms_len.append(s["ms_length"])
+            ms_samp.append(s["ms_sample"])
+            n_newton.append(s["n_newton"])
+            n_panels.append(s["n_panels"])
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = float(sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    launches = calc.stats()["n_launches"] - launches0
+    ms_per_step = total_ms / args.steps
+    value = world * n_curves / (ms_per_step * 1e-3)
+    samples_per_s = world * n_samples / (ms_per_step * 1e-3)
+
+    # ---- accuracy of this run on a subset (vs the oracle) --------------------
+    # (reported, not asserted: tests/ carry the parity bars)
+    # ---- roofline of the dominant kernel ------------------------------------
+    fpe = flops_per_eval(batch)
+    samp_flops = float(np.mean(n_newton)) * (8 * (fpe + 4.0) + fpe + 4.0) + n_samples * 20.0
+    len_flops = float(np.mean(n_panels)) * (16 * (fpe + 2.0) + 40.0)
+    ms_s, ms_l = float(np.mean(ms_samp)), float(np.mean(ms_len))
+    fp64_peak = _lib.measure_fma_peak(0)
+    fp32_peak = _lib.measure_fma_peak(1)
+    if ms_s >= ms_l:
+        dom, flops, ms = "k_sample", samp_flops, ms_s
+        bytes_alg = n_samples * (8 + 8 + 8) + n_curves * 8
+    else:
+        dom, flops, ms = "k_length", len_flops, ms_l
+        bytes_alg = batch.knots.nbytes + batch.ctrl.nbytes + batch.n_segments.sum() * 8
+    achieved = flops / (ms * 1e-3) / 1e12
+    peak = fp64_peak if precision == g.GCV_PLAIN_FP64 else fp32_peak
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_per_unit.json")
+    if os.path.exists(prof):
+        try:
+            tpu = json.load(open(prof)).get(f"{dom}:{args.workload}:{args.precision}")
+            if tpu:
+                traffic = float(tpu) * (n_samples if dom == "k_sample" else float(batch.n_segments.sum()))
+        except (ValueError, OSError):
+            traffic = None
+    hbm_peak = None
+    mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(mp):
+        hbm_peak = json.load(open(mp)).get("hbm_gbs")
+    roofline = {
+        "kernel": dom, "bound": "fp64" if precision == g.GCV_PLAIN_FP64 else "fp32",
+        "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
+        "frac": round(achieved / peak, 4), "peak_source": "measured in-run by gcv_measure_fma_peak (FMA probe kernel)",
+        "traffic": traffic, "ms_per_launch": round(ms, 4), "algorithmic_flops_per_launch": flops,
+        "hbm": {"achieved_gbs": round(bytes_alg / (ms * 1e-3) / 1e9, 2), "peak_gbs": hbm_peak,
+                "frac": round(bytes_alg / (ms * 1e-3) / 1e9 / hbm_peak, 4) if hbm_peak else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "phases_ms": {"length": round(ms_l, 4), "sample": round(ms_s, 4)},
+        "fp32_peak_tflops": round(fp32_peak, 2),
+    }
+    calc.close()
+
+    # ---- end-to-end through the public API with host buffers -----------------
+    e2e_t = []
+    h_out = np.empty(n_samples, np.float64)
+    for i in range(max(args.e2e_steps, 1) + 1):
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        c2 = g.ArclengthCalculateGpu.from_batch(batch, precision=precision)
+        c2.createArclengthTable()
+        c2.arclengthReverseInto(batch.n_samples, pos, h_out, True, g.GCV_RETURN_US)
+        c2.close()
+        dt = time.perf_counter() - t0
+        if i > 0:
+            e2e_t.append(dt)
+    e2e_s = float(np.mean(e2e_t))
+    if dist:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2d = batch.nbytes() + batch.n_samples.nbytes + pos.nbytes
+    d2h = h_out.nbytes
+
+    # ---- CPU baseline (rank 0, N = 1 only) -----------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        nthreads = os.cpu_count() or 1
+        sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch))
+        secs, kind = run_cpu_reference(sub, nthreads)
+        cpu = {"value": round(sub.n_curve / secs, 3), "unit": "curves/s", "cores": nthreads, "kind": kind,
+               "sample": f"{sub.n_curve} curves of the workload ({sub.total_samples} samples), table + sampling, "
+                         f"{secs:.2f} s", "samples_per_s": round(sub.total_samples / secs, 1)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "curves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == g.GCV_PLAIN_FP64 else "f32+f64",
+            "data": "synthetic: seeded generator (numpy default_rng, seed = rank)",
+            "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][1]}",
+                       "precision": args.precision, "rtol": 1e-10 if precision == g.GCV_PLAIN_FP64 else 1e-8,
+                       "curves_per_gpu": n_curves, "samples_per_gpu": n_samples,
+                       "l2": "flushed between timed steps (256 MB write, untimed)",
+                       "parallelism": f"replicas x{world} (independent curves, no collective)"},
+            "samples_per_s": round(samples_per_s, 1),
+            "e2e": {"value": round(world * n_curves / e2e_s, 3), "unit": "curves/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "samples_per_s": round(world * n_samples / e2e_s, 1),
+                    "ms_per_step": round(e2e_s * 1e3, 3)},
+            "gpu_launches": int(launches),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def reference_arm(args):
+    nthreads = os.cpu_count() or 1
+    batch = make_batch(args.workload, seed=0)
+    sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch))
+    times, kind = [], None
+    for i in range(max(args.warmup, 3) + args.steps):
+        secs, kind = run_cpu_reference(sub, nthreads)
+        if i >= max(args.warmup, 3):
+            times.append(secs)
+    per = float(np.mean(times))
+    value = sub.n_curve / per
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "curves/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(per * 1e3, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded generator (numpy default_rng, seed 0)",
+        "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][1]}", "precision": "plain",
+                   "sample_curves": sub.n_curve},
+        "samples_per_s": round(sub.total_samples / per, 1),
+        "cpu_baseline": {"value": round(value, 3), "unit": "curves/s", "cores": nthreads, "kind": kind,
+                         "sample": f"{sub.n_curve} curves of the workload ({sub.total_samples} samples) per step, "
+                                   "table + sampling, all host threads"},
+        "e2e": {"value": round(value, 3), "unit": "curves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,142 @@
+"""ctypes binding of libgcurval_gb300.so (include/gcurval_gb300.h).
+
+The library is the only compute path: if it is missing or a GPU is absent the
+calls fail with GcvError; nothing falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libgcurval_gb300.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "gcurval_gb300.h")
+
+GCV_OK = 0
+GCV_ERR_INVALID = 1
+GCV_ERR_CUDA = 2
+GCV_ERR_OUT_OF_MEMORY = 3
+GCV_ERR_STATE = 4
+GCV_ERR_OVERFLOW = 5
+GCV_ERR_TIMEOUT = 6
+GCV_ERR_NO_DEVICE = 7
+
+GCV_DEVICE = 0
+GCV_HOST = 1
+GCV_RETURN_US = 2
+GCV_RETURN_POINTS = 3
+
+GCV_PLAIN_FP64 = 0
+GCV_MIXED = 1
+
+STATUS_NAMES = {0: "GCV_OK", 1: "GCV_ERR_INVALID", 2: "GCV_ERR_CUDA", 3: "GCV_ERR_OUT_OF_MEMORY",
+                4: "GCV_ERR_STATE", 5: "GCV_ERR_OVERFLOW", 6: "GCV_ERR_TIMEOUT", 7: "GCV_ERR_NO_DEVICE"}
+
+_P = ctypes.c_void_p
+
+
+class GcvError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("rtol", ctypes.c_double), ("max_depth", ctypes.c_int), ("precision", ctypes.c_int),
+                ("stream", _P), ("collect_stats", ctypes.c_int)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("n_points", ctypes.c_int64), ("store_where", ctypes.c_int), ("store_what", ctypes.c_int),
+                ("point_dim", ctypes.c_int), ("data", _P)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_curves", ctypes.c_int64), ("n_segments", ctypes.c_int64), ("n_leaves", ctypes.c_int64),
+                ("n_panels", ctypes.c_int64), ("n_deep_segments", ctypes.c_int64), ("n_capped", ctypes.c_int64),
+                ("n_samples", ctypes.c_int64), ("n_newton", ctypes.c_int64), ("ms_setup", ctypes.c_double),
+                ("ms_length", ctypes.c_double), ("ms_scan", ctypes.c_double), ("ms_sample", ctypes.c_double),
+                ("n_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_SIGS = {
+    "gcv_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "gcv_last_error": (ctypes.c_char_p, []),
+    "gcv_version": (ctypes.c_int, []),
+    "gcv_default_options": (ctypes.c_int, [ctypes.POINTER(Options), ctypes.c_int]),
+    "gcv_create_ellipses": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_int,
+                                           ctypes.POINTER(Options)]),
+    "gcv_create_bsplines": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
+                                           ctypes.c_int, ctypes.POINTER(Options)]),
+    "gcv_create_batch": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, _P, _P, _P, _P, _P, _P, _P, ctypes.c_int,
+                                        ctypes.POINTER(Options)]),
+    "gcv_destroy": (ctypes.c_int, [_P]),
+    "gcv_set_options": (ctypes.c_int, [_P, ctypes.POINTER(Options)]),
+    "gcv_create_arclength_table": (ctypes.c_int, [_P]),
+    "gcv_get_all_curve_arclengths": (ctypes.c_int, [_P, _P, ctypes.c_int]),
+    "gcv_get_arclength": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "gcv_arclength_reverse": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                             ctypes.POINTER(Result)]),
+    "gcv_arclength_reverse_into": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P,
+                                                  ctypes.c_int]),
+    "gcv_free_result": (ctypes.c_int, [ctypes.POINTER(Result)]),
+    "gcv_clear_arclength": (ctypes.c_int, [_P]),
+    "gcv_synchronize": (ctypes.c_int, [_P]),
+    "gcv_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
+    "gcv_get_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                     ctypes.POINTER(ctypes.c_int)]),
+    "gcv_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+}
+
+_lib = None
+
+
+def declared_symbols(header: str = HEADER):
+    """Names of the functions include/gcurval_gb300.h declares."""
+    import re
+    txt = open(header).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(gcv_[a-z0-9_]+)\s*\(", txt)))
+
+
+def load(path: str = LIB_PATH):
+    """Loads the library (building it first when only the sources exist)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        from . import build as _build
+        _build.build()
+    if not os.path.exists(path):
+        raise GcvError(GCV_ERR_NO_DEVICE, f"{path} is missing; build it with python -m gcurval_gb300.build")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(status: int) -> None:
+    if status != GCV_OK:
+        msg = _lib.gcv_last_error().decode() if _lib is not None else ""
+        raise GcvError(status, msg)
+
+
+def measure_fma_peak(which: int) -> float:
+    """FMA throughput of the current GPU in TFLOP/s (0: FP64, 1: FP32)."""
+    lib = load()
+    v = ctypes.c_double()
+    check(lib.gcv_measure_fma_peak(int(which), ctypes.byref(v)))
+    return v.value
+
+
+def default_options(precision: int = GCV_PLAIN_FP64) -> Options:
+    lib = load()
+    o = Options()
+    check(lib.gcv_default_options(ctypes.byref(o), precision))
+    return o

@@ -1,0 +1,1025 @@
+// C ABI of the arc-length library (include/gcurval_gb300.h): contexts, device
+// memory, and the host-side orchestration of the set-up, length, scan and
+// sampling kernels on the context's stream.
+#include "gcurval_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gcv_kernels.cuh"
+#include "gcv_mixed.cuh"
+
+using namespace gcv;
+
+namespace {
+
+thread_local std::string g_err;
+
+gcv_status fail(gcv_status s, const std::string& msg)
+{
+    g_err = msg;
+    return s;
+}
+
+gcv_status cuda_fail(cudaError_t e, const char* what)
+{
+    cudaGetLastError();
+    const gcv_status s = e == cudaErrorMemoryAllocation ? GCV_ERR_OUT_OF_MEMORY
+                       : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver || e == cudaErrorNoKernelImageForDevice)
+                           ? GCV_ERR_NO_DEVICE
+                           : GCV_ERR_CUDA;
+    return fail(s, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call);                                        \
+    } while (0)
+
+#define CHECK(st)                                                                                  \
+    do {                                                                                           \
+        gcv_status s_ = (st);                                                                      \
+        if (s_ != GCV_OK) return s_;                                                               \
+    } while (0)
+
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    bool owned = true;
+
+    gcv_status reserve(size_t count)
+    {
+        if (count <= n && p) return GCV_OK;
+        release();
+        if (count == 0) count = 1;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            n = 0;
+            return cuda_fail(e, "cudaMalloc");
+        }
+        n = count;
+        owned = true;
+        return GCV_OK;
+    }
+    void borrow(const T* q, size_t count)
+    {
+        release();
+        p = const_cast<T*>(q);
+        n = count;
+        owned = false;
+    }
+    void release()
+    {
+        if (p && owned) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        owned = true;
+    }
+};
+
+template <typename T>
+gcv_status upload(DBuf<T>& b, const T* h, size_t count, cudaStream_t st)
+{
+    CHECK(b.reserve(count));
+    if (count) CU(cudaMemcpyAsync(b.p, h, count * sizeof(T), cudaMemcpyHostToDevice, st));
+    return GCV_OK;
+}
+
+int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+}  // namespace
+
+struct gcv_ctx {
+    gcv_options opt{};
+    cudaStream_t stream = nullptr;
+    int64_t n_curve = 0, n_seg = 0, n_coef = 0;
+    int point_dim = 2;
+    int code = -1;  // common curve code, -1 when the batch mixes codes
+
+    // batch (owned or borrowed)
+    DBuf<uint8_t> kind, degree, dim;
+    DBuf<int64_t> knot_off, ctrl_off;
+    DBuf<double> knots, ctrl;
+    // derived
+    DBuf<int64_t> seg_off, coef_off;
+    DBuf<int> seg_curve;
+    std::vector<int64_t> h_seg_off;
+    std::vector<uint8_t> h_kind, h_degree;
+    std::vector<double> h_start;  // first parameter value of each curve
+
+    // table
+    DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_len, seg_cum, curve_len;
+    DBuf<int64_t> leaf_off;
+    DBuf<int> leaf_cnt;
+    DBuf<double> leaf_v, leaf_cum, leaf_f;
+    int64_t leaf_cap = 0;
+    DBuf<int> deep_list;
+    DBuf<unsigned long long> ctr;
+    DBuf<int> scan_status, scan_flag;
+    DBuf<double> scan_hi, scan_lo;
+    bool table_ready = false;
+    mixed::MixedState mixed;
+
+    // sampling scratch
+    DBuf<int64_t> sample_off;
+    DBuf<int> sample_cnt;
+    DBuf<double> sample_pos, sample_out;
+    std::vector<int64_t> h_sample_off;
+
+    std::vector<double> h_len;
+    bool h_len_valid = false;
+    unsigned long long* h_ctr = nullptr;  // pinned
+    gcv_stats stats{};
+    cudaEvent_t ev[8] = {};
+    bool ev_table = false, ev_sample = false;
+};
+
+namespace {
+
+Batch batch_view(gcv_ctx* c)
+{
+    Batch b;
+    b.n_curve = c->n_curve;
+    b.n_seg = c->n_seg;
+    b.kind = c->kind.p;
+    b.degree = c->degree.p;
+    b.dim = c->dim.p;
+    b.knot_off = c->knot_off.p;
+    b.knots = c->knots.p;
+    b.ctrl_off = c->ctrl_off.p;
+    b.ctrl = c->ctrl.p;
+    b.seg_off = c->seg_off.p;
+    b.coef_off = c->coef_off.p;
+    b.seg_curve = c->seg_curve.p;
+    return b;
+}
+
+Table table_view(gcv_ctx* c)
+{
+    Table t;
+    t.coef = c->coef.p;
+    t.seg_t0 = c->seg_t0.p;
+    t.seg_t1 = c->seg_t1.p;
+    t.seg_f0 = c->seg_f0.p;
+    t.seg_len = c->seg_len.p;
+    t.seg_cum = c->seg_cum.p;
+    t.curve_len = c->curve_len.p;
+    t.leaf_off = c->leaf_off.p;
+    t.leaf_cnt = c->leaf_cnt.p;
+    t.leaf_v = c->leaf_v.p;
+    t.leaf_cum = c->leaf_cum.p;
+    t.leaf_f = c->leaf_f.p;
+    t.leaf_cap = c->leaf_cap;
+    t.deep_list = c->deep_list.p;
+    t.deep_cap = (int64_t)c->deep_list.n;
+    t.ctr = c->ctr.p;
+    t.scan_status = c->scan_status.p;
+    t.scan_flag = c->scan_flag.p;
+    t.scan_hi = c->scan_hi.p;
+    t.scan_lo = c->scan_lo.p;
+    return t;
+}
+
+gcv_status check_options(const gcv_options* o)
+{
+    if (!o) return fail(GCV_ERR_INVALID, "options are NULL");
+    if (!(o->rtol > 0.0) || !(o->rtol < 1.0)) return fail(GCV_ERR_INVALID, "rtol must be in (0, 1)");
+    if (o->max_depth < 1 || o->max_depth > MAX_DEPTH_LIMIT)
+        return fail(GCV_ERR_INVALID, "max_depth must be in [1, " + std::to_string(MAX_DEPTH_LIMIT) + "]");
+    if (o->precision != GCV_PLAIN_FP64 && o->precision != GCV_MIXED)
+        return fail(GCV_ERR_INVALID, "unknown precision mode");
+    return GCV_OK;
+}
+
+void destroy_ctx(gcv_ctx* c)
+{
+    if (!c) return;
+    c->kind.release();
+    c->degree.release();
+    c->dim.release();
+    c->knot_off.release();
+    c->ctrl_off.release();
+    c->knots.release();
+    c->ctrl.release();
+    c->seg_off.release();
+    c->coef_off.release();
+    c->seg_curve.release();
+    c->coef.release();
+    c->seg_t0.release();
+    c->seg_t1.release();
+    c->seg_f0.release();
+    c->seg_len.release();
+    c->seg_cum.release();
+    c->curve_len.release();
+    c->leaf_off.release();
+    c->leaf_cnt.release();
+    c->leaf_v.release();
+    c->leaf_cum.release();
+    c->leaf_f.release();
+    c->deep_list.release();
+    c->ctr.release();
+    c->scan_status.release();
+    c->scan_flag.release();
+    c->scan_hi.release();
+    c->scan_lo.release();
+    c->sample_off.release();
+    c->sample_cnt.release();
+    c->sample_pos.release();
+    c->sample_out.release();
+    mixed::release(c->mixed);
+    if (c->h_ctr) cudaFreeHost(c->h_ctr);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    delete c;
+}
+
+// Validates per-curve metadata on the host and derives segment / coefficient
+// offsets.  knot_off and ctrl_off are int64 prefix arrays of length n + 1.
+gcv_status derive_layout(gcv_ctx* c, const uint8_t* kind, const uint8_t* degree, const uint8_t* dim,
+                         const int64_t* knot_off, const int64_t* ctrl_off, std::vector<int64_t>& seg_off,
+                         std::vector<int64_t>& coef_off)
+{
+    const int64_t n = c->n_curve;
+    seg_off.assign(n + 1, 0);
+    coef_off.assign(n + 1, 0);
+    int common = -2, pdim = 0;
+    bool mixed_dim = false;
+    if (knot_off[0] != 0 || ctrl_off[0] != 0) return fail(GCV_ERR_INVALID, "offsets must start at 0");
+    for (int64_t i = 0; i < n; ++i) {
+        const int64_t nk = knot_off[i + 1] - knot_off[i];
+        const int64_t nc = ctrl_off[i + 1] - ctrl_off[i];
+        int64_t ns = 0;
+        int code = 0, d = 2;
+        if (kind[i] == GCV_KIND_ELLIPSE) {
+            if (nk != 2 || nc != 5)
+                return fail(GCV_ERR_INVALID, "curve " + std::to_string(i) + ": an ellipse has 2 knots and 5 control values");
+            ns = 1;
+            code = CODE_ELLIPSE;
+        } else if (kind[i] == GCV_KIND_BSPLINE) {
+            const int p = degree[i];
+            d = dim[i];
+            if (p < 1 || p > MAX_DEGREE)
+                return fail(GCV_ERR_INVALID, "curve " + std::to_string(i) + ": degree must be in [1, 5]");
+            if (d != 2 && d != 3) return fail(GCV_ERR_INVALID, "curve " + std::to_string(i) + ": dim must be 2 or 3");
+            ns = nk - 2 * p - 1;
+            if (ns < 0)
+                return fail(GCV_ERR_INVALID, "curve " + std::to_string(i) + ": fewer than 2 * degree + 1 knots");
+            if (nc != (nk - p - 1) * d)
+                return fail(GCV_ERR_INVALID,
+                            "curve " + std::to_string(i) + ": control values must be (knots - degree - 1) * dim");
+            code = bs_code(p, d);
+        } else {
+            return fail(GCV_ERR_INVALID, "curve " + std::to_string(i) + ": unknown kind");
+        }
+        if (nk < 0 || nc < 0) return fail(GCV_ERR_INVALID, "offsets must be non-decreasing");
+        seg_off[i + 1] = seg_off[i] + ns;
+        coef_off[i + 1] = coef_off[i] + ns * code_stride(code);
+        if (common == -2)
+            common = code;
+        else if (common != code)
+            common = -1;
+        if (pdim == 0)
+            pdim = d;
+        else if (pdim != d)
+            mixed_dim = true;
+    }
+    c->n_seg = seg_off[n];
+    c->n_coef = coef_off[n];
+    c->code = common >= 0 ? common : -1;
+    c->point_dim = mixed_dim ? 3 : (pdim ? pdim : 2);
+    if (c->n_seg > (int64_t)0x7fffffff) return fail(GCV_ERR_INVALID, "more than 2^31 - 1 knot intervals");
+    return GCV_OK;
+}
+
+gcv_status finish_create(gcv_ctx* c, const uint8_t* kind, const uint8_t* degree, const uint8_t* dim,
+                         const int64_t* knot_off, const int64_t* ctrl_off, const double* knots_host_or_null)
+{
+    std::vector<int64_t> seg_off, coef_off;
+    CHECK(derive_layout(c, kind, degree, dim, knot_off, ctrl_off, seg_off, coef_off));
+    c->h_seg_off = seg_off;
+    c->h_kind.assign(kind, kind + c->n_curve);
+    c->h_degree.assign(degree, degree + c->n_curve);
+    (void)knots_host_or_null;
+    CHECK(upload(c->seg_off, seg_off.data(), seg_off.size(), c->stream));
+    CHECK(upload(c->coef_off, coef_off.data(), coef_off.size(), c->stream));
+    CHECK(c->seg_curve.reserve((size_t)std::max<int64_t>(c->n_seg, 1)));
+    CHECK(c->ctr.reserve(C_COUNT));
+    CU(cudaMallocHost(&c->h_ctr, C_COUNT * sizeof(unsigned long long)));
+    for (auto& e : c->ev) CU(cudaEventCreate(&e));
+    if (c->n_curve > 0) {
+        const Batch b = batch_view(c);
+        const int blocks = (int)std::min<int64_t>((c->n_curve + 255) / 256, 65535);
+        k_seg_curve<<<blocks, 256, 0, c->stream>>>(b, c->seg_curve.p);
+        CU(cudaGetLastError());
+        c->stats.n_launches++;
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    c->stats.n_curves = c->n_curve;
+    c->stats.n_segments = c->n_seg;
+    return GCV_OK;
+}
+
+gcv_status new_ctx(gcv_ctx** out, int n_curve, const gcv_options* opt, gcv_ctx** made)
+{
+    if (!out) return fail(GCV_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (n_curve < 0) return fail(GCV_ERR_INVALID, "n_curve < 0");
+    gcv_options o;
+    gcv_default_options(&o, opt ? opt->precision : GCV_PLAIN_FP64);
+    if (opt) o = *opt;
+    CHECK(check_options(&o));
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) return fail(GCV_ERR_NO_DEVICE, "no CUDA device is available");
+    gcv_ctx* c = new gcv_ctx();
+    c->opt = o;
+    c->stream = (cudaStream_t)o.stream;
+    c->n_curve = n_curve;
+    *made = c;
+    return GCV_OK;
+}
+
+template <typename T>
+gcv_status to_host(const T* src, size_t n, int where, std::vector<T>& dst)
+{
+    dst.resize(n);
+    if (!n) return GCV_OK;
+    if (where == GCV_HOST)
+        std::memcpy(dst.data(), src, n * sizeof(T));
+    else
+        CU(cudaMemcpy(dst.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost));
+    return GCV_OK;
+}
+
+// ------------------------------------------------------------ table build
+
+gcv_status ensure_table_buffers(gcv_ctx* c)
+{
+    const size_t ns = (size_t)std::max<int64_t>(c->n_seg, 1);
+    CHECK(c->coef.reserve((size_t)std::max<int64_t>(c->n_coef, 1)));
+    CHECK(c->seg_t0.reserve(ns));
+    CHECK(c->seg_t1.reserve(ns));
+    CHECK(c->seg_f0.reserve(ns));
+    CHECK(c->seg_len.reserve(ns));
+    CHECK(c->seg_cum.reserve(ns));
+    CHECK(c->leaf_off.reserve(ns));
+    CHECK(c->leaf_cnt.reserve(ns));
+    CHECK(c->curve_len.reserve((size_t)std::max<int64_t>(c->n_curve, 1)));
+    if (c->leaf_cap == 0) {
+        c->leaf_cap = 2 * (int64_t)ns + 4096;
+        CHECK(c->leaf_v.reserve((size_t)c->leaf_cap));
+        CHECK(c->leaf_cum.reserve((size_t)c->leaf_cap));
+        CHECK(c->leaf_f.reserve((size_t)c->leaf_cap));
+    }
+    if (c->deep_list.n == 0) CHECK(c->deep_list.reserve(ns / 64 + 1024));
+    const size_t tiles = (ns + SCAN_TILE - 1) / SCAN_TILE;
+    CHECK(c->scan_status.reserve(tiles));
+    CHECK(c->scan_flag.reserve(tiles));
+    CHECK(c->scan_hi.reserve(tiles));
+    CHECK(c->scan_lo.reserve(tiles));
+    return GCV_OK;
+}
+
+// grows the leaf pool to `cap`, keeping the first `keep` leaves
+gcv_status grow_pool(gcv_ctx* c, int64_t cap, int64_t keep)
+{
+    DBuf<double>* bufs[3] = {&c->leaf_v, &c->leaf_cum, &c->leaf_f};
+    for (DBuf<double>* b : bufs) {
+        DBuf<double> nb;
+        CHECK(nb.reserve((size_t)cap));
+        if (keep > 0) CU(cudaMemcpyAsync(nb.p, b->p, (size_t)keep * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+        b->release();
+        *b = nb;
+        nb.p = nullptr;
+        nb.n = 0;
+    }
+    c->leaf_cap = cap;
+    return GCV_OK;
+}
+
+gcv_status read_counters(gcv_ctx* c)
+{
+    CU(cudaMemcpyAsync(c->h_ctr, c->ctr.p, C_COUNT * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return GCV_OK;
+}
+
+template <int MODE>
+gcv_status launch_length(gcv_ctx* c, const LengthParams& P)
+{
+    int occ = 0;
+    cudaError_t e;
+    switch (c->code) {
+    case CODE_ELLIPSE:
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, CODE_ELLIPSE>, LK_THREADS, 0);
+        break;
+    case bs_code(3, 2):
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, bs_code(3, 2)>, LK_THREADS, 0);
+        break;
+    case bs_code(3, 3):
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, bs_code(3, 3)>, LK_THREADS, 0);
+        break;
+    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, -1>, LK_THREADS, 0); break;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
+    occ = std::max(1, std::min(occ, 16));
+    int64_t want = (P.n_items + LK_HALVES - 1) / LK_HALVES;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * occ, want));
+    switch (c->code) {
+    case CODE_ELLIPSE: k_length<MODE, CODE_ELLIPSE><<<grid, LK_THREADS, 0, c->stream>>>(P); break;
+    case bs_code(3, 2): k_length<MODE, bs_code(3, 2)><<<grid, LK_THREADS, 0, c->stream>>>(P); break;
+    case bs_code(3, 3): k_length<MODE, bs_code(3, 3)><<<grid, LK_THREADS, 0, c->stream>>>(P); break;
+    default: k_length<MODE, -1><<<grid, LK_THREADS, 0, c->stream>>>(P); break;
+    }
+    CU(cudaGetLastError());
+    c->stats.n_launches++;
+    return GCV_OK;
+}
+
+gcv_status build_table_fp64(gcv_ctx* c)
+{
+    CHECK(ensure_table_buffers(c));
+    const Batch b = batch_view(c);
+    const int setup_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 64));
+    CU(cudaEventRecord(c->ev[0], c->stream));
+    CU(cudaMemsetAsync(c->ctr.p, 0, C_COUNT * sizeof(unsigned long long), c->stream));
+    if (c->n_seg > 0) {
+        k_setup<<<setup_blocks, 256, 0, c->stream>>>(b, table_view(c));
+        CU(cudaGetLastError());
+        c->stats.n_launches++;
+    }
+    CU(cudaEventRecord(c->ev[1], c->stream));
+    for (int attempt = 0;; ++attempt) {
+        if (attempt > 8) return fail(GCV_ERR_OVERFLOW, "leaf pool kept overflowing");
+        // keep the set-up's error bits, clear the rest
+        CU(cudaMemsetAsync(c->ctr.p, 0, C_ERR * sizeof(unsigned long long), c->stream));
+        LengthParams P;
+        P.b = b;
+        P.t = table_view(c);
+        P.rtol = c->opt.rtol;
+        P.max_depth = c->opt.max_depth;
+        P.collect = c->opt.collect_stats;
+        P.list = nullptr;
+        P.n_items = c->n_seg;
+        if (c->n_seg > 0) CHECK(launch_length<0>(c, P));
+        CHECK(read_counters(c));
+        const unsigned long long err = c->h_ctr[C_ERR];
+        if (err & ERR_BAD_KNOTS) return fail(GCV_ERR_INVALID, "knot vector decreases or holds NaN");
+        if (err & ERR_POOL) {
+            CHECK(grow_pool(c, (int64_t)(c->h_ctr[C_LEAF_TOP] * 1.25) + 4096, 0));
+            CU(cudaMemsetAsync(c->ctr.p + C_ERR, 0, sizeof(unsigned long long), c->stream));
+            continue;
+        }
+        if (err & ERR_DEEP_LIST) {
+            DBuf<int>& dl = c->deep_list;
+            const size_t need = (size_t)(c->h_ctr[C_DEEP] * 1.25) + 1024;
+            dl.release();
+            CHECK(dl.reserve(need));
+            CU(cudaMemsetAsync(c->ctr.p + C_ERR, 0, sizeof(unsigned long long), c->stream));
+            continue;
+        }
+        const int64_t n_deep = (int64_t)c->h_ctr[C_DEEP];
+        int64_t top = (int64_t)c->h_ctr[C_LEAF_TOP];
+        if (n_deep > 0) {
+            // count pass
+            CU(cudaMemsetAsync(c->ctr.p + C_WORK, 0, sizeof(unsigned long long), c->stream));
+            LengthParams Q = P;
+            Q.t = table_view(c);
+            Q.list = c->deep_list.p;
+            Q.n_items = n_deep;
+            Q.collect = 0;
+            CHECK(launch_length<1>(c, Q));
+            // total leaves of the deep segments: sum leaf_cnt over the list
+            std::vector<int> ids((size_t)n_deep);
+            CU(cudaMemcpyAsync(ids.data(), c->deep_list.p, (size_t)n_deep * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            std::vector<int> cnt((size_t)c->n_seg);
+            CU(cudaMemcpyAsync(cnt.data(), c->leaf_cnt.p, (size_t)c->n_seg * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+            CU(cudaStreamSynchronize(c->stream));
+            int64_t extra = 0;
+            for (int s : ids) extra += cnt[(size_t)s];
+            if (top + extra > c->leaf_cap) CHECK(grow_pool(c, top + extra + 4096, top));
+            CU(cudaMemsetAsync(c->ctr.p + C_WORK, 0, sizeof(unsigned long long), c->stream));
+            Q.t = table_view(c);
+            Q.collect = P.collect;
+            CHECK(launch_length<2>(c, Q));
+            CHECK(read_counters(c));
+            if (c->h_ctr[C_ERR] & ERR_POOL) return fail(GCV_ERR_OVERFLOW, "leaf pool overflow in the deep pass");
+            top = (int64_t)c->h_ctr[C_LEAF_TOP];
+        }
+        c->stats.n_leaves = top;
+        c->stats.n_deep_segments = n_deep;
+        c->stats.n_panels = (int64_t)c->h_ctr[C_PANELS];
+        c->stats.n_capped = (int64_t)c->h_ctr[C_CAPPED];
+        break;
+    }
+    CU(cudaEventRecord(c->ev[2], c->stream));
+    const int64_t tiles = (c->n_seg + SCAN_TILE - 1) / SCAN_TILE;
+    if (tiles > 0) {
+        CU(cudaMemsetAsync(c->scan_status.p, 0, (size_t)tiles * sizeof(int), c->stream));
+        CU(cudaMemsetAsync(c->ctr.p + C_SCAN_TILE, 0, sizeof(unsigned long long), c->stream));
+        k_scan<<<(unsigned)tiles, SCAN_THREADS, 0, c->stream>>>(b, table_view(c), tiles);
+        CU(cudaGetLastError());
+        c->stats.n_launches++;
+    }
+    if (c->n_curve > 0) {
+        k_curve_len<<<(unsigned)std::min<int64_t>((c->n_curve + 255) / 256, 65535), 256, 0, c->stream>>>(b, table_view(c));
+        CU(cudaGetLastError());
+        c->stats.n_launches++;
+    }
+    CU(cudaEventRecord(c->ev[3], c->stream));
+    c->ev_table = true;
+    return GCV_OK;
+}
+
+// ---------------------------------------------------------------- sampling
+
+gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, const double* d_pos, int64_t total, int is_relative,
+                        int what, double* d_out)
+{
+    if (total == 0) return GCV_OK;
+    CU(cudaEventRecord(c->ev[4], c->stream));
+    if (c->opt.collect_stats) CU(cudaMemsetAsync(c->ctr.p + C_NEWTON, 0, sizeof(unsigned long long), c->stream));
+    if (c->opt.precision == GCV_MIXED) {
+        CHECK(mixed::sample(c->mixed, c->stream, batch_view(c), table_view(c), d_sample_off, d_pos, total, is_relative,
+                            what, c->point_dim, d_out, c->opt.collect_stats));
+    } else {
+        SampleParams P;
+        P.b = batch_view(c);
+        P.t = table_view(c);
+        P.sample_off = d_sample_off;
+        P.pos = d_pos;
+        P.is_relative = is_relative;
+        P.what = what;
+        P.pdim = c->point_dim;
+        P.out = d_out;
+        P.n_samples = total;
+        P.collect = c->opt.collect_stats;
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((total + SAMPLE_THREADS - 1) / SAMPLE_THREADS,
+                                                                   (int64_t)sm_count() * 64));
+        switch (c->code) {
+        case CODE_ELLIPSE: k_sample<CODE_ELLIPSE><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+        case bs_code(3, 2): k_sample<bs_code(3, 2)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+        case bs_code(3, 3): k_sample<bs_code(3, 3)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+        default: k_sample<-1><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+        }
+        CU(cudaGetLastError());
+        c->stats.n_launches++;
+    }
+    CU(cudaEventRecord(c->ev[5], c->stream));
+    c->ev_sample = true;
+    c->stats.n_samples = total;
+    return GCV_OK;
+}
+
+gcv_status stage_counts(gcv_ctx* c, const int* n_ptrs, int in_where, int64_t* total)
+{
+    const int64_t n = c->n_curve;
+    std::vector<int> cnt;
+    CHECK(to_host(n_ptrs, (size_t)n, in_where, cnt));
+    std::vector<int64_t>& off = c->h_sample_off;
+    off.assign((size_t)n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        if (cnt[(size_t)i] < 0) return fail(GCV_ERR_INVALID, "negative sample count");
+        off[(size_t)i + 1] = off[(size_t)i] + cnt[(size_t)i];
+    }
+    *total = off[(size_t)n];
+    CHECK(upload(c->sample_off, off.data(), off.size(), c->stream));
+    return GCV_OK;
+}
+
+}  // namespace
+
+// ===================================================================== ABI
+
+extern "C" {
+
+const char* gcv_status_string(gcv_status s)
+{
+    switch (s) {
+    case GCV_OK: return "ok";
+    case GCV_ERR_INVALID: return "invalid argument";
+    case GCV_ERR_CUDA: return "CUDA error";
+    case GCV_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case GCV_ERR_STATE: return "invalid state";
+    case GCV_ERR_OVERFLOW: return "device structure overflow";
+    case GCV_ERR_TIMEOUT: return "bounded device wait timed out";
+    case GCV_ERR_NO_DEVICE: return "no usable CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* gcv_last_error(void) { return g_err.c_str(); }
+
+int gcv_version(void) { return 100; }
+
+gcv_status gcv_default_options(gcv_options* opt, int precision)
+{
+    if (!opt) return fail(GCV_ERR_INVALID, "opt is NULL");
+    std::memset(opt, 0, sizeof(*opt));
+    opt->precision = precision;
+    opt->rtol = precision == GCV_MIXED ? 1e-8 : 1e-10;
+    opt->max_depth = 30;
+    opt->stream = nullptr;
+    opt->collect_stats = 0;
+    return GCV_OK;
+}
+
+gcv_status gcv_create_batch(gcv_ctx** out, int n_curve, const uint8_t* kind, const uint8_t* degree, const uint8_t* dim,
+                            const int64_t* knot_off, const double* knots, const int64_t* ctrl_off, const double* ctrl,
+                            int where, const gcv_options* opt)
+{
+    gcv_ctx* c = nullptr;
+    CHECK(new_ctx(out, n_curve, opt, &c));
+    if (where != GCV_HOST && where != GCV_DEVICE) {
+        destroy_ctx(c);
+        return fail(GCV_ERR_INVALID, "where must be GCV_HOST or GCV_DEVICE");
+    }
+    if (n_curve > 0 && (!kind || !degree || !dim || !knot_off || !ctrl_off)) {
+        destroy_ctx(c);
+        return fail(GCV_ERR_INVALID, "NULL curve array");
+    }
+    std::vector<uint8_t> hk, hd, hm;
+    std::vector<int64_t> hko, hco;
+    gcv_status st;
+    if ((st = to_host(kind, (size_t)n_curve, where, hk)) != GCV_OK ||
+        (st = to_host(degree, (size_t)n_curve, where, hd)) != GCV_OK ||
+        (st = to_host(dim, (size_t)n_curve, where, hm)) != GCV_OK ||
+        (st = to_host(knot_off, (size_t)n_curve + 1, where, hko)) != GCV_OK ||
+        (st = to_host(ctrl_off, (size_t)n_curve + 1, where, hco)) != GCV_OK) {
+        destroy_ctx(c);
+        return st;
+    }
+    if (n_curve == 0) {
+        hko.assign(1, 0);
+        hco.assign(1, 0);
+    }
+    const int64_t nk = hko[(size_t)n_curve], nc = hco[(size_t)n_curve];
+    if ((nk > 0 && !knots) || (nc > 0 && !ctrl)) {
+        destroy_ctx(c);
+        return fail(GCV_ERR_INVALID, "NULL knots or control array");
+    }
+    if (where == GCV_HOST) {
+        if ((st = upload(c->kind, hk.data(), hk.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->degree, hd.data(), hd.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->dim, hm.data(), hm.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->knot_off, hko.data(), hko.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->ctrl_off, hco.data(), hco.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->knots, knots, (size_t)nk, c->stream)) != GCV_OK ||
+            (st = upload(c->ctrl, ctrl, (size_t)nc, c->stream)) != GCV_OK) {
+            destroy_ctx(c);
+            return st;
+        }
+    } else {
+        c->kind.borrow(kind, (size_t)n_curve);
+        c->degree.borrow(degree, (size_t)n_curve);
+        c->dim.borrow(dim, (size_t)n_curve);
+        c->knot_off.borrow(knot_off, (size_t)n_curve + 1);
+        c->ctrl_off.borrow(ctrl_off, (size_t)n_curve + 1);
+        c->knots.borrow(knots, (size_t)nk);
+        c->ctrl.borrow(ctrl, (size_t)nc);
+    }
+    if ((st = finish_create(c, hk.data(), hd.data(), hm.data(), hko.data(), hco.data(), nullptr)) != GCV_OK) {
+        destroy_ctx(c);
+        return st;
+    }
+    *out = c;
+    return GCV_OK;
+}
+
+gcv_status gcv_create_bsplines(gcv_ctx** out, int n_curve, int degree, int dim, const int* knots_offset,
+                               const double* knot_vector, const double* ctrl_pts, int where, const gcv_options* opt)
+{
+    if (!out) return fail(GCV_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (n_curve < 0) return fail(GCV_ERR_INVALID, "n_curve < 0");
+    if (degree < 1 || degree > MAX_DEGREE) return fail(GCV_ERR_INVALID, "degree must be in [1, 5]");
+    if (dim != 2 && dim != 3) return fail(GCV_ERR_INVALID, "dim must be 2 or 3");
+    if (!knots_offset) return fail(GCV_ERR_INVALID, "knots_offset is NULL");
+    std::vector<int> ko;
+    CHECK(to_host(knots_offset, (size_t)n_curve + 1, where == GCV_DEVICE ? GCV_DEVICE : GCV_HOST, ko));
+    std::vector<uint8_t> k((size_t)n_curve, GCV_KIND_BSPLINE), dg((size_t)n_curve, (uint8_t)degree),
+        dm((size_t)n_curve, (uint8_t)dim);
+    std::vector<int64_t> knot_off((size_t)n_curve + 1), ctrl_off((size_t)n_curve + 1);
+    for (int i = 0; i <= n_curve; ++i) {
+        knot_off[(size_t)i] = ko[(size_t)i];
+        // the sample's layout: curve c's control points start at knots_offset[c] - (degree + 1) c
+        ctrl_off[(size_t)i] = ((int64_t)ko[(size_t)i] - (int64_t)(degree + 1) * i) * dim;
+    }
+    if (where == GCV_DEVICE) {
+        // metadata is small: copy it, but keep the caller's knots and control points
+        gcv_ctx* c = nullptr;
+        CHECK(new_ctx(out, n_curve, opt, &c));
+        gcv_status st;
+        if ((st = upload(c->kind, k.data(), k.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->degree, dg.data(), dg.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->dim, dm.data(), dm.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->knot_off, knot_off.data(), knot_off.size(), c->stream)) != GCV_OK ||
+            (st = upload(c->ctrl_off, ctrl_off.data(), ctrl_off.size(), c->stream)) != GCV_OK) {
+            destroy_ctx(c);
+            return st;
+        }
+        c->knots.borrow(knot_vector, (size_t)knot_off.back());
+        c->ctrl.borrow(ctrl_pts, (size_t)ctrl_off.back());
+        if ((st = finish_create(c, k.data(), dg.data(), dm.data(), knot_off.data(), ctrl_off.data(), nullptr)) != GCV_OK) {
+            destroy_ctx(c);
+            return st;
+        }
+        *out = c;
+        return GCV_OK;
+    }
+    return gcv_create_batch(out, n_curve, k.data(), dg.data(), dm.data(), knot_off.data(), knot_vector, ctrl_off.data(),
+                            ctrl_pts, GCV_HOST, opt);
+}
+
+gcv_status gcv_create_ellipses(gcv_ctx** out, int n_curve, const double* a, const double* b, const double* rot,
+                               const double* cx, const double* cy, int where, const gcv_options* opt)
+{
+    if (!out) return fail(GCV_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (n_curve < 0) return fail(GCV_ERR_INVALID, "n_curve < 0");
+    if (n_curve > 0 && (!a || !b)) return fail(GCV_ERR_INVALID, "a or b is NULL");
+    const int w = where == GCV_DEVICE ? GCV_DEVICE : GCV_HOST;
+    std::vector<double> ha, hb, hr, hx, hy;
+    CHECK(to_host(a, (size_t)n_curve, w, ha));
+    CHECK(to_host(b, (size_t)n_curve, w, hb));
+    if (rot) CHECK(to_host(rot, (size_t)n_curve, w, hr));
+    if (cx) CHECK(to_host(cx, (size_t)n_curve, w, hx));
+    if (cy) CHECK(to_host(cy, (size_t)n_curve, w, hy));
+    std::vector<uint8_t> k((size_t)n_curve, GCV_KIND_ELLIPSE), dg((size_t)n_curve, 0), dm((size_t)n_curve, 2);
+    std::vector<int64_t> ko((size_t)n_curve + 1), co((size_t)n_curve + 1);
+    std::vector<double> knots((size_t)n_curve * 2), ctrl((size_t)n_curve * 5);
+    for (int i = 0; i < n_curve; ++i) {
+        ko[(size_t)i] = 2 * (int64_t)i;
+        co[(size_t)i] = 5 * (int64_t)i;
+        knots[2 * (size_t)i] = 0.0;
+        knots[2 * (size_t)i + 1] = 2.0 * PI;
+        ctrl[5 * (size_t)i + 0] = ha[(size_t)i];
+        ctrl[5 * (size_t)i + 1] = hb[(size_t)i];
+        ctrl[5 * (size_t)i + 2] = rot ? hr[(size_t)i] : 0.0;
+        ctrl[5 * (size_t)i + 3] = cx ? hx[(size_t)i] : 0.0;
+        ctrl[5 * (size_t)i + 4] = cy ? hy[(size_t)i] : 0.0;
+    }
+    ko[(size_t)n_curve] = 2 * (int64_t)n_curve;
+    co[(size_t)n_curve] = 5 * (int64_t)n_curve;
+    return gcv_create_batch(out, n_curve, k.data(), dg.data(), dm.data(), ko.data(), knots.data(), co.data(), ctrl.data(),
+                            GCV_HOST, opt);
+}
+
+gcv_status gcv_destroy(gcv_ctx* ctx)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    else cudaDeviceSynchronize();
+    destroy_ctx(ctx);
+    return GCV_OK;
+}
+
+gcv_status gcv_set_options(gcv_ctx* ctx, const gcv_options* opt)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    CHECK(check_options(opt));
+    const bool rebuild = opt->precision != ctx->opt.precision || opt->rtol != ctx->opt.rtol ||
+                         opt->max_depth != ctx->opt.max_depth;
+    ctx->opt = *opt;
+    ctx->stream = (cudaStream_t)opt->stream;
+    if (rebuild) {
+        ctx->table_ready = false;
+        ctx->h_len_valid = false;
+    }
+    return GCV_OK;
+}
+
+gcv_status gcv_create_arclength_table(gcv_ctx* ctx)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    ctx->table_ready = false;
+    ctx->h_len_valid = false;
+    if (ctx->opt.precision == GCV_MIXED) {
+        CHECK(ensure_table_buffers(ctx));
+        CHECK(mixed::build_table(ctx->mixed, ctx->stream, batch_view(ctx), table_view(ctx), ctx->code, ctx->opt.rtol,
+                                 ctx->opt.max_depth, ctx->opt.collect_stats, ctx->ev, &ctx->stats, ctx->h_ctr,
+                                 ctx->leaf_cap));
+    } else {
+        CHECK(build_table_fp64(ctx));
+    }
+    ctx->table_ready = true;
+    return GCV_OK;
+}
+
+gcv_status gcv_get_all_curve_arclengths(gcv_ctx* ctx, double* out, int where)
+{
+    if (!ctx || !out) return fail(GCV_ERR_INVALID, "NULL argument");
+    if (!ctx->table_ready) return fail(GCV_ERR_STATE, "createArclengthTable has not run");
+    if (ctx->n_curve == 0) return GCV_OK;
+    const size_t bytes = (size_t)ctx->n_curve * sizeof(double);
+    if (where == GCV_DEVICE) {
+        CU(cudaMemcpyAsync(out, ctx->curve_len.p, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    } else {
+        CU(cudaMemcpyAsync(out, ctx->curve_len.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+    }
+    return GCV_OK;
+}
+
+gcv_status gcv_get_arclength(gcv_ctx* ctx, int cid, double* out)
+{
+    if (!ctx || !out) return fail(GCV_ERR_INVALID, "NULL argument");
+    if (!ctx->table_ready) return fail(GCV_ERR_STATE, "createArclengthTable has not run");
+    if (cid < 0 || cid >= ctx->n_curve) return fail(GCV_ERR_INVALID, "cid out of range");
+    if (!ctx->h_len_valid) {
+        ctx->h_len.resize((size_t)ctx->n_curve);
+        CHECK(gcv_get_all_curve_arclengths(ctx, ctx->h_len.data(), GCV_HOST));
+        ctx->h_len_valid = true;
+    }
+    *out = ctx->h_len[(size_t)cid];
+    return GCV_OK;
+}
+
+gcv_status gcv_clear_arclength(gcv_ctx* ctx)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    ctx->h_len.clear();
+    ctx->h_len.shrink_to_fit();
+    ctx->h_len_valid = false;
+    return GCV_OK;
+}
+
+gcv_status gcv_arclength_reverse_into(gcv_ctx* ctx, const int* n_ptrs_for_curves, const double* sample_position,
+                                      int is_relative, int in_where, int what, double* out, int out_where)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    if (!ctx->table_ready) return fail(GCV_ERR_STATE, "createArclengthTable has not run");
+    if (what != GCV_RETURN_US && what != GCV_RETURN_POINTS) return fail(GCV_ERR_INVALID, "what must be RETURN_US or RETURN_POINTS");
+    if (in_where != GCV_HOST && in_where != GCV_DEVICE) return fail(GCV_ERR_INVALID, "bad in_where");
+    if (out_where != GCV_HOST && out_where != GCV_DEVICE) return fail(GCV_ERR_INVALID, "bad out_where");
+    if (ctx->n_curve > 0 && !n_ptrs_for_curves) return fail(GCV_ERR_INVALID, "n_ptrs_for_curves is NULL");
+    int64_t total = 0;
+    CHECK(stage_counts(ctx, n_ptrs_for_curves, in_where, &total));
+    if (total == 0) return GCV_OK;
+    if (!sample_position || !out) return fail(GCV_ERR_INVALID, "NULL positions or output");
+    const double* d_pos = sample_position;
+    if (in_where == GCV_HOST) {
+        CHECK(upload(ctx->sample_pos, sample_position, (size_t)total, ctx->stream));
+        d_pos = ctx->sample_pos.p;
+    }
+    const int width = what == GCV_RETURN_US ? 1 : ctx->point_dim;
+    double* d_out = out;
+    if (out_where == GCV_HOST) {
+        CHECK(ctx->sample_out.reserve((size_t)total * width));
+        d_out = ctx->sample_out.p;
+    }
+    CHECK(run_sampling(ctx, ctx->sample_off.p, d_pos, total, is_relative ? 1 : 0, what, d_out));
+    if (out_where == GCV_HOST) {
+        CU(cudaMemcpyAsync(out, d_out, (size_t)total * width * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+    }
+    return GCV_OK;
+}
+
+gcv_status gcv_arclength_reverse(gcv_ctx* ctx, const int* n_ptrs_for_curves, const double* sample_position,
+                                 int is_relative, int where, int what, gcv_result* result)
+{
+    if (!ctx || !result) return fail(GCV_ERR_INVALID, "NULL argument");
+    std::memset(result, 0, sizeof(*result));
+    if (!ctx->table_ready) return fail(GCV_ERR_STATE, "createArclengthTable has not run");
+    if (where != GCV_HOST && where != GCV_DEVICE) return fail(GCV_ERR_INVALID, "where must be GCV_HOST or GCV_DEVICE");
+    if (what != GCV_RETURN_US && what != GCV_RETURN_POINTS) return fail(GCV_ERR_INVALID, "what must be RETURN_US or RETURN_POINTS");
+    if (ctx->n_curve > 0 && !n_ptrs_for_curves) return fail(GCV_ERR_INVALID, "n_ptrs_for_curves is NULL");
+    int64_t total = 0;
+    for (int64_t i = 0; i < ctx->n_curve; ++i) {
+        if (n_ptrs_for_curves[i] < 0) return fail(GCV_ERR_INVALID, "negative sample count");
+        total += n_ptrs_for_curves[i];
+    }
+    const int width = what == GCV_RETURN_US ? 1 : ctx->point_dim;
+    result->n_points = total;
+    result->store_where = where;
+    result->store_what = what;
+    result->point_dim = what == GCV_RETURN_US ? 1 : ctx->point_dim;
+    const size_t bytes = (size_t)std::max<int64_t>(total, 1) * width * sizeof(double);
+    if (where == GCV_DEVICE) {
+        CU(cudaMalloc(&result->data, bytes));
+    } else {
+        result->data = (double*)std::malloc(bytes);
+        if (!result->data) return fail(GCV_ERR_OUT_OF_MEMORY, "host result allocation failed");
+    }
+    gcv_status st = gcv_arclength_reverse_into(ctx, n_ptrs_for_curves, sample_position, is_relative, GCV_HOST, what,
+                                               result->data, where);
+    if (st != GCV_OK) {
+        gcv_free_result(result);
+        return st;
+    }
+    if (where == GCV_DEVICE) CU(cudaStreamSynchronize(ctx->stream));
+    return GCV_OK;
+}
+
+gcv_status gcv_free_result(gcv_result* r)
+{
+    if (!r) return fail(GCV_ERR_INVALID, "result is NULL");
+    if (r->data) {
+        if (r->store_where == GCV_DEVICE)
+            cudaFree(r->data);
+        else
+            std::free(r->data);
+    }
+    r->data = nullptr;
+    r->n_points = 0;
+    return GCV_OK;
+}
+
+gcv_status gcv_synchronize(gcv_ctx* ctx)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    CU(cudaStreamSynchronize(ctx->stream));
+    return GCV_OK;
+}
+
+gcv_status gcv_get_stats(gcv_ctx* ctx, gcv_stats* out)
+{
+    if (!ctx || !out) return fail(GCV_ERR_INVALID, "NULL argument");
+    CU(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    if (ctx->ev_table) {
+        if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]) == cudaSuccess) ctx->stats.ms_setup = ms;
+        if (cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]) == cudaSuccess) ctx->stats.ms_length = ms;
+        if (cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]) == cudaSuccess) ctx->stats.ms_scan = ms;
+    }
+    if (ctx->ev_sample) {
+        if (cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]) == cudaSuccess) ctx->stats.ms_sample = ms;
+        if (ctx->opt.collect_stats) {
+            CHECK(read_counters(ctx));
+            ctx->stats.n_newton = (int64_t)ctx->h_ctr[C_NEWTON];
+        }
+    }
+    cudaGetLastError();
+    *out = ctx->stats;
+    return GCV_OK;
+}
+
+gcv_status gcv_measure_fma_peak(int which, double* tflops)
+{
+    if (!tflops || (which != 0 && which != 1)) return fail(GCV_ERR_INVALID, "which must be 0 (FP64) or 1 (FP32)");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(GCV_ERR_NO_DEVICE, "no CUDA device is available");
+    }
+    const int threads = 256, blocks = sm_count() * 8;
+    const int iters = which == 0 ? 256 : 16384;
+    void* out = nullptr;
+    CU(cudaMalloc(&out, 16));
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; ++rep) {
+        CU(cudaEventRecord(e0));
+        if (which == 0)
+            k_fma_probe<double><<<blocks, threads>>>((double*)out, iters, 1.0);
+        else
+            k_fma_probe<float><<<blocks, threads>>>((float*)out, iters, 1.0f);
+        CU(cudaGetLastError());
+        CU(cudaEventRecord(e1));
+        CU(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) best = std::min(best, ms);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    const double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return GCV_OK;
+}
+
+gcv_status gcv_get_shape(gcv_ctx* ctx, int64_t* n_curve, int64_t* n_segments, int* point_dim)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    if (n_curve) *n_curve = ctx->n_curve;
+    if (n_segments) *n_segments = ctx->n_seg;
+    if (point_dim) *point_dim = ctx->point_dim;
+    return GCV_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,691 @@
+// Kernels of the FP64 arc-length path (set-up, adaptive length, scan,
+// sampling) and their parameter blocks.  Included by gcv_kernels.cu, which
+// instantiates them, and by the header-only plugin path.
+#pragma once
+
+#include "gcv_device.cuh"
+
+namespace gcv {
+
+// ----------------------------------------------------------- device views
+struct Batch {
+    int64_t n_curve;
+    int64_t n_seg;
+    const uint8_t* kind;
+    const uint8_t* degree;
+    const uint8_t* dim;
+    const int64_t* knot_off;
+    const double* knots;
+    const int64_t* ctrl_off;
+    const double* ctrl;
+    const int64_t* seg_off;   // [n_curve + 1] first segment of each curve
+    const int64_t* coef_off;  // [n_curve + 1] first coefficient (double) of each curve
+    const int* seg_curve;     // [n_seg] curve of each segment
+};
+
+// counters in one device array (reset before each phase that uses them)
+enum Counter {
+    C_WORK = 0,       // length work-queue head
+    C_LEAF_TOP = 1,   // leaf-pool bump pointer
+    C_DEEP = 2,       // number of segments on the deep list
+    C_PANELS = 3,
+    C_CAPPED = 4,
+    C_NEWTON = 5,
+    C_ERR = 6,        // error bits (ERR_*)
+    C_NONFINITE = 7,
+    C_SCAN_TILE = 8,  // scan tile ticket
+    C_COUNT = 16
+};
+enum ErrBits { ERR_POOL = 1, ERR_SCAN_TIMEOUT = 2, ERR_BAD_KNOTS = 4, ERR_DEEP_LIST = 8 };
+
+struct Table {
+    double* coef;      // per-segment evaluation data (code_stride doubles)
+    double* seg_t0;    // curve parameter at v = -1
+    double* seg_t1;    // curve parameter at v = +1
+    double* seg_f0;    // f(-1)
+    double* seg_len;   // length of each segment
+    double* seg_cum;   // cumulative length at the end of each segment (within its curve)
+    double* curve_len;
+    int64_t* leaf_off;
+    int* leaf_cnt;
+    double* leaf_v;    // right end (local v) of each leaf panel
+    double* leaf_cum;  // cumulative length within the segment at that end
+    double* leaf_f;    // f at that end
+    int64_t leaf_cap;
+    int* deep_list;
+    int64_t deep_cap;
+    unsigned long long* ctr;
+    int* scan_status;  // per scan tile: 0 none, 1 aggregate, 2 inclusive
+    int* scan_flag;
+    double* scan_hi;
+    double* scan_lo;
+};
+
+__device__ __forceinline__ int curve_code(const Batch& b, int64_t c)
+{
+    return b.kind[c] == 0 ? CODE_ELLIPSE : bs_code(b.degree[c], b.dim[c]);
+}
+
+__device__ __forceinline__ void raise_err(const Table& t, unsigned bits)
+{
+    atomicOr(t.ctr + C_ERR, (unsigned long long)bits);
+}
+
+// ---------------------------------------------------------------- set-up
+// One thread per segment: segment -> curve map consumer; writes the
+// evaluation data of the segment (B-spline polynomials or ellipse terms).
+template <int P, int D>
+__device__ void setup_bspline_seg(const Batch& b, const Table& t, int64_t s, int64_t c)
+{
+    const int64_t j = s - b.seg_off[c];
+    const double* kv = b.knots + b.knot_off[c];
+    const double* cp = b.ctrl + b.ctrl_off[c];
+    const int span = int(j) + P;
+    double* out = t.coef + b.coef_off[c] + j * code_stride(bs_code(P, D));
+    const double ka = kv[span], kb = kv[span + 1];
+    if (!(kb >= ka)) raise_err(t, ERR_BAD_KNOTS);
+    if (kb > ka) {
+        bspline_setup<P, D>(kv, cp, span, out);
+        t.seg_t0[s] = ka;
+        t.seg_t1[s] = kb;
+        t.seg_f0[s] = Eval<bs_code(P, D)>::speed(out + (P + 1) * D, -1.0);
+    } else {
+        for (int i = 0; i < code_stride(bs_code(P, D)); ++i) out[i] = 0.0;
+        t.seg_t0[s] = ka;
+        t.seg_t1[s] = ka;
+        t.seg_f0[s] = 0.0;
+    }
+}
+
+__device__ inline void setup_ellipse_seg(const Batch& b, const Table& t, int64_t s, int64_t c)
+{
+    const double* e = b.ctrl + b.ctrl_off[c];
+    double* out = t.coef + b.coef_off[c];
+    const double a = e[0], bb = e[1];
+    double sr, cr;
+    sincos(e[2], &sr, &cr);
+    out[0] = a * a - bb * bb;
+    out[1] = bb * bb;
+    out[2] = a;
+    out[3] = bb;
+    out[4] = cr;
+    out[5] = sr;
+    out[6] = e[3];
+    out[7] = e[4];
+    t.seg_t0[s] = 0.0;
+    t.seg_t1[s] = 2.0 * PI;
+    t.seg_f0[s] = PI * fabs(bb);
+}
+
+__global__ void k_setup(Batch b, Table t)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < b.n_seg;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = b.seg_curve[s];
+        switch (curve_code(b, c)) {
+        case CODE_ELLIPSE: setup_ellipse_seg(b, t, s, c); break;
+#define GCV_SETUP_CASE(P, D)                                                                       \
+    case bs_code(P, D): setup_bspline_seg<P, D>(b, t, s, c); break;
+            GCV_SETUP_CASE(1, 2) GCV_SETUP_CASE(2, 2) GCV_SETUP_CASE(3, 2) GCV_SETUP_CASE(4, 2)
+            GCV_SETUP_CASE(5, 2) GCV_SETUP_CASE(1, 3) GCV_SETUP_CASE(2, 3) GCV_SETUP_CASE(3, 3)
+            GCV_SETUP_CASE(4, 3) GCV_SETUP_CASE(5, 3)
+#undef GCV_SETUP_CASE
+        default: break;
+        }
+    }
+}
+
+// segment -> curve map (thread per curve writes its range)
+__global__ void k_seg_curve(Batch b, int* seg_curve)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < b.n_curve;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t s = b.seg_off[c]; s < b.seg_off[c + 1]; ++s) seg_curve[s] = int(c);
+    }
+}
+
+// ------------------------------------------------------ adaptive length
+// Persistent half-warp workers.  A half-warp (16 lanes) owns one segment at a
+// time and refines it depth-first: each iteration evaluates one panel with
+// the 15-node Kronrod rule (lanes 0..14) plus the panel's right end (lane 15),
+// reduces K15 and G7 with an xor butterfly, and either accepts the panel
+// (|K15 - G7| within the panel's share of rtol * length) or splits it,
+// pushing the right half on a shared-memory stack.  Accepted panels leave in
+// parameter order and are staged in shared memory, then copied to the leaf
+// pool at an atomically reserved offset.  Segments with more than LCAP leaves
+// go to a deep list and are redone by the MODE 1 (count) / MODE 2 (write)
+// passes, which write straight to the pool.
+constexpr int LK_THREADS = 128;
+constexpr int LK_HALVES = LK_THREADS / 16;
+constexpr int STACK_CAP = 40;
+constexpr int LCAP = 48;
+constexpr int LK_CHUNK = 4;
+constexpr long long PANEL_BUDGET = 1ll << 22;
+constexpr int MAX_DEPTH_LIMIT = STACK_CAP - 2;
+
+struct LengthParams {
+    Batch b;
+    Table t;
+    double rtol;
+    int max_depth;
+    int collect;
+    const int* list;  // segments to process (deep passes); NULL: all segments
+    int64_t n_items;
+};
+
+template <int MODE, int CODE>
+__global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
+{
+    __shared__ double st_v[LK_HALVES][STACK_CAP];
+    __shared__ int st_d[LK_HALVES][STACK_CAP];
+    __shared__ double lf_v[MODE == 0 ? LK_HALVES : 1][MODE == 0 ? LCAP : 1];
+    __shared__ double lf_c[MODE == 0 ? LK_HALVES : 1][MODE == 0 ? LCAP : 1];
+    __shared__ double lf_f[MODE == 0 ? LK_HALVES : 1][MODE == 0 ? LCAP : 1];
+
+    const Batch& b = P.b;
+    const Table& t = P.t;
+    const int lane = threadIdx.x & 31;
+    const int hl = lane & 15;
+    const int half = threadIdx.x >> 4;
+    const unsigned hmask = (lane < 16) ? 0x0000FFFFu : 0xFFFF0000u;
+    const int hbase = lane & 16;
+    double xn, wk, wg;
+    gk_lane(hl, xn, wk, wg);
+    const double eps50 = 50.0 * 2.220446049250313e-16;
+
+    int64_t next = 0, end = 0;
+    unsigned long long my_panels = 0, my_capped = 0, my_nonfinite = 0;
+
+    for (;;) {
+        if (next == end) {
+            unsigned long long base = 0;
+            if (hl == 0) base = atomicAdd(t.ctr + C_WORK, (unsigned long long)LK_CHUNK);
+            base = __shfl_sync(hmask, base, hbase);
+            if ((int64_t)base >= P.n_items) break;
+            next = (int64_t)base;
+            end = min((int64_t)base + LK_CHUNK, P.n_items);
+        }
+        const int64_t item = next++;
+        const int64_t s = P.list ? (int64_t)P.list[item] : item;
+        const int64_t c = b.seg_curve[s];
+        const int code = CODE >= 0 ? CODE : curve_code(b, c);
+        const double* seg = t.coef + b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
+        double r[MAX_COEF];
+        if constexpr (CODE >= 0)
+            Eval<(CODE >= 0 ? CODE : 0)>::load_speed(seg, r);
+        else
+            load_speed_dyn(code, seg, r);
+
+        int64_t pool = 0;
+        if (MODE == 2) {
+            unsigned long long o = 0;
+            if (hl == 0) o = atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)t.leaf_cnt[s]);
+            pool = (int64_t)__shfl_sync(hmask, o, hbase);
+            if (pool + t.leaf_cnt[s] > t.leaf_cap) {
+                if (hl == 0) raise_err(t, ERR_POOL);
+                continue;
+            }
+        }
+
+        if (t.seg_t1[s] == t.seg_t0[s]) {  // zero-width knot interval: one empty leaf
+            if (MODE == 0) {
+                unsigned long long o = 0;
+                if (hl == 0) o = atomicAdd(t.ctr + C_LEAF_TOP, 1ull);
+                o = __shfl_sync(hmask, o, hbase);
+                if (hl == 0) {
+                    if ((int64_t)o < t.leaf_cap) {
+                        t.leaf_v[o] = 1.0;
+                        t.leaf_cum[o] = 0.0;
+                        t.leaf_f[o] = 0.0;
+                    } else {
+                        raise_err(t, ERR_POOL);
+                    }
+                    t.seg_len[s] = 0.0;
+                    t.leaf_off[s] = (int64_t)o;
+                    t.leaf_cnt[s] = 1;
+                }
+            } else if (hl == 0) {
+                if (MODE == 1) t.leaf_cnt[s] = 1;
+                if (MODE == 2) {
+                    t.leaf_v[pool] = 1.0;
+                    t.leaf_cum[pool] = 0.0;
+                    t.leaf_f[pool] = 0.0;
+                    t.seg_len[s] = 0.0;
+                    t.leaf_off[s] = pool;
+                }
+            }
+            continue;
+        }
+
+        double v_lo = -1.0, cum = 0.0, tol_unit = 0.0;
+        int depth = 0, sp = 0, nleaf = 0;
+        long long panels = 0;
+        bool overflow = false;
+        for (;;) {
+            const double hw = pow2_neg(depth);
+            const double mid = v_lo + hw;
+            const double v = fma(hw, xn, mid);
+            double f;
+            if constexpr (CODE >= 0)
+                f = Eval<(CODE >= 0 ? CODE : 0)>::speed(r, v);
+            else
+                f = speed_dyn(code, r, v);
+            const double K = half_sum(f * wk, hmask) * hw;
+            const double G = half_sum(f * wg, hmask) * hw;
+            const double fend = __shfl_sync(hmask, f, hbase + 15);
+            if (depth == 0) tol_unit = P.rtol * fabs(K);
+            const double err = fabs(K - G);
+            ++panels;
+            const bool finite = isfinite(K) && isfinite(G);
+            const bool at_cap = depth >= P.max_depth || panels >= PANEL_BUDGET;
+            const bool ok = err <= fmax(tol_unit * hw, eps50 * fabs(K));
+            if (ok || at_cap || !finite) {
+                if (!ok && finite) ++my_capped;
+                if (!finite) ++my_nonfinite;
+                cum += K;
+                const double vr = v_lo + 2.0 * hw;
+                if (MODE == 0) {
+                    if (nleaf < LCAP) {
+                        if (hl == 0) {
+                            lf_v[half][nleaf] = vr;
+                            lf_c[half][nleaf] = cum;
+                            lf_f[half][nleaf] = fend;
+                        }
+                    } else {
+                        overflow = true;
+                        break;
+                    }
+                } else if (MODE == 2) {
+                    if (hl == 0) {
+                        t.leaf_v[pool + nleaf] = vr;
+                        t.leaf_cum[pool + nleaf] = cum;
+                        t.leaf_f[pool + nleaf] = fend;
+                    }
+                }
+                ++nleaf;
+                if (sp == 0) break;
+                --sp;
+                v_lo = st_v[half][sp];
+                depth = st_d[half][sp];
+            } else {
+                if (hl == 0) {
+                    st_v[half][sp] = mid;
+                    st_d[half][sp] = depth + 1;
+                }
+                __syncwarp(hmask);
+                ++sp;
+                ++depth;
+            }
+        }
+        my_panels += panels;
+
+        if (MODE == 0) {
+            if (overflow) {
+                unsigned long long o = 0;
+                if (hl == 0) o = atomicAdd(t.ctr + C_DEEP, 1ull);
+                o = __shfl_sync(hmask, o, hbase);
+                if (hl == 0) {
+                    if ((int64_t)o < t.deep_cap)
+                        t.deep_list[o] = int(s);
+                    else
+                        raise_err(t, ERR_DEEP_LIST);
+                }
+                continue;
+            }
+            __syncwarp(hmask);
+            unsigned long long o = 0;
+            if (hl == 0) o = atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)nleaf);
+            o = __shfl_sync(hmask, o, hbase);
+            if ((int64_t)o + nleaf <= t.leaf_cap) {
+                for (int i = hl; i < nleaf; i += 16) {
+                    t.leaf_v[o + i] = lf_v[half][i];
+                    t.leaf_cum[o + i] = lf_c[half][i];
+                    t.leaf_f[o + i] = lf_f[half][i];
+                }
+            } else if (hl == 0) {
+                raise_err(t, ERR_POOL);
+            }
+            if (hl == 0) {
+                t.seg_len[s] = cum;
+                t.leaf_off[s] = (int64_t)o;
+                t.leaf_cnt[s] = nleaf;
+            }
+            __syncwarp(hmask);
+        } else if (MODE == 1) {
+            if (hl == 0) t.leaf_cnt[s] = nleaf;
+        } else {
+            if (hl == 0) {
+                t.seg_len[s] = cum;
+                t.leaf_off[s] = pool;
+            }
+        }
+    }
+    if (hl == 0 && (P.collect || my_capped || my_nonfinite)) {
+        if (P.collect) atomicAdd(t.ctr + C_PANELS, my_panels);
+        if (my_capped) atomicAdd(t.ctr + C_CAPPED, my_capped);
+        if (my_nonfinite) atomicAdd(t.ctr + C_NONFINITE, my_nonfinite);
+    }
+}
+
+// ------------------------------------------------- compensated scan
+// Single-pass segmented inclusive scan of segment lengths (segments of one
+// curve are contiguous; a curve's first segment starts a new sum) with
+// decoupled look-back between tiles and double-double (two-sum) arithmetic,
+// replacing the reference's per-segment Brent-Kung scan plus one thread per
+// curve doing a sequential Kahan sum (gcurval/detail/cuda/kernel/generic.inl.cuh:52-137).
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr long long SCAN_SPIN_LIMIT = 1ll << 22;
+
+struct DD {
+    double hi, lo;
+};
+__device__ __forceinline__ DD dd_add(DD a, DD b)
+{
+    const double s = a.hi + b.hi;
+    const double bb = s - a.hi;
+    double e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    const double h = s + e;
+    return DD{h, e - (h - s)};
+}
+struct SegVal {
+    int flag;  // a curve starts inside this range
+    DD v;      // sum since the last start
+};
+// a earlier, b later
+__device__ __forceinline__ SegVal seg_combine(const SegVal& a, const SegVal& b)
+{
+    if (b.flag) return b;
+    return SegVal{a.flag, dd_add(a.v, b.v)};
+}
+__device__ __forceinline__ SegVal shfl_up_sv(const SegVal& x, int d)
+{
+    SegVal y;
+    y.flag = __shfl_up_sync(0xffffffffu, x.flag, d);
+    y.v.hi = __shfl_up_sync(0xffffffffu, x.v.hi, d);
+    y.v.lo = __shfl_up_sync(0xffffffffu, x.v.lo, d);
+    return y;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, int64_t n_tiles)
+{
+    __shared__ int s_tile;
+    __shared__ SegVal s_warp[SCAN_THREADS / 32];
+    __shared__ SegVal s_prefix;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(t.ctr + C_SCAN_TILE, 1ull);
+    __syncthreads();
+    const int64_t tile = s_tile;
+    if (tile >= n_tiles) return;
+    const int64_t base = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+
+    double x[SCAN_ITEMS];
+    int head[SCAN_ITEMS];
+    int prev_curve = base > 0 && base - 1 < b.n_seg ? b.seg_curve[base - 1] : -1;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const int64_t s = base + k;
+        if (s < b.n_seg) {
+            x[k] = t.seg_len[s];
+            const int cc = b.seg_curve[s];
+            head[k] = (s == 0) || cc != prev_curve;
+            prev_curve = cc;
+        } else {
+            x[k] = 0.0;
+            head[k] = 0;
+        }
+    }
+    // thread aggregate
+    SegVal agg{0, DD{0.0, 0.0}};
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) agg = seg_combine(agg, SegVal{head[k], DD{x[k], 0.0}});
+    // warp inclusive scan of aggregates
+    SegVal inc = agg;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const SegVal y = shfl_up_sv(inc, d);
+        if (lane >= d) inc = seg_combine(y, inc);
+    }
+    if (lane == 31) s_warp[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        SegVal w = lane < SCAN_THREADS / 32 ? s_warp[lane] : SegVal{0, DD{0.0, 0.0}};
+#pragma unroll
+        for (int d = 1; d < SCAN_THREADS / 32; d <<= 1) {
+            const SegVal y = shfl_up_sv(w, d);
+            if (lane >= d) w = seg_combine(y, w);
+        }
+        if (lane < SCAN_THREADS / 32) s_warp[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    // exclusive prefix of this thread inside the tile
+    SegVal excl = shfl_up_sv(inc, 1);
+    if (lane == 0) excl = SegVal{0, DD{0.0, 0.0}};
+    if (warp > 0) excl = lane == 0 ? s_warp[warp - 1] : seg_combine(s_warp[warp - 1], excl);
+
+    // decoupled look-back by thread 0
+    if (threadIdx.x == 0) {
+        const SegVal tile_agg = s_warp[SCAN_THREADS / 32 - 1];
+        SegVal pre{0, DD{0.0, 0.0}};
+        if (tile == 0) {
+            pre = SegVal{1, DD{0.0, 0.0}};
+        } else {
+            t.scan_flag[tile] = tile_agg.flag;
+            t.scan_hi[tile] = tile_agg.v.hi;
+            t.scan_lo[tile] = tile_agg.v.lo;
+            __threadfence();
+            atomicExch(t.scan_status + tile, 1);
+            bool done = false;
+            for (int64_t j = tile - 1; j >= 0 && !done; --j) {
+                int st = 0;
+                for (long long it = 0; it < SCAN_SPIN_LIMIT; ++it) {
+                    st = atomicAdd(t.scan_status + j, 0);
+                    if (st) break;
+                    __nanosleep(64);
+                }
+                if (!st) {
+                    raise_err(t, ERR_SCAN_TIMEOUT);
+                    break;
+                }
+                __threadfence();
+                const SegVal pj{__ldcg(t.scan_flag + j), DD{__ldcg(t.scan_hi + j), __ldcg(t.scan_lo + j)}};
+                pre = seg_combine(pj, pre);
+                if (st == 2 || pj.flag) done = true;
+            }
+        }
+        const SegVal incl = seg_combine(pre, tile_agg);
+        t.scan_flag[tile] = 1;
+        t.scan_hi[tile] = incl.v.hi;
+        t.scan_lo[tile] = incl.v.lo;
+        __threadfence();
+        atomicExch(t.scan_status + tile, 2);
+        s_prefix = pre;
+    }
+    __syncthreads();
+    SegVal run = seg_combine(s_prefix, excl);
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        run = seg_combine(run, SegVal{head[k], DD{x[k], 0.0}});
+        const int64_t s = base + k;
+        if (s < b.n_seg) t.seg_cum[s] = run.v.hi + run.v.lo;
+    }
+}
+
+__global__ void k_curve_len(Batch b, Table t)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < b.n_curve;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = b.seg_off[c + 1];
+        t.curve_len[c] = e > b.seg_off[c] ? t.seg_cum[e - 1] : 0.0;
+    }
+}
+
+// ------------------------------------------------------------- sampling
+// One thread per sample: curve by binary search of the sample offsets,
+// segment by binary search of the cumulative segment table, leaf panel by
+// binary search of the segment's leaves, then Newton on
+//   F(v) = S(v_a) + GL8(v_a, v) - r
+// from a cubic-Hermite guess of the inverse map, safeguarded by bisection.
+struct SampleParams {
+    Batch b;
+    Table t;
+    const int64_t* sample_off;  // [n_curve + 1]
+    const double* pos;
+    int is_relative;
+    int what;  // 2 = parameters, 3 = points
+    int pdim;
+    double* out;
+    int64_t n_samples;
+    int collect;
+};
+
+constexpr int SAMPLE_THREADS = 256;
+constexpr int NEWTON_MAXIT = 16;
+
+template <int CODE>
+__device__ __forceinline__ double speed_of(int code, const double* r, double v)
+{
+    if constexpr (CODE >= 0)
+        return Eval<CODE>::speed(r, v);
+    else
+        return speed_dyn(code, r, v);
+}
+
+template <int CODE>
+__global__ void __launch_bounds__(SAMPLE_THREADS) k_sample(SampleParams P)
+{
+    const Batch& b = P.b;
+    const Table& t = P.t;
+    unsigned long long newton = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n_samples;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = upper_bound_i64(P.sample_off, int(b.n_curve) + 1, i);
+        const int code = CODE >= 0 ? CODE : curve_code(b, c);
+        const int64_t s0 = b.seg_off[c], s1 = b.seg_off[c + 1];
+        int64_t s;
+        double v;
+        if (s1 == s0) {  // curve without knot intervals: its start
+            s = -1;
+            v = -1.0;
+        } else {
+            const double L = t.curve_len[c];
+            const double pos = P.pos[i];
+            const double target = P.is_relative ? pos * L : pos;
+            if (!(target > 0.0)) {
+                s = s0;
+                v = -1.0;
+            } else if (target >= L) {
+                s = s1 - 1;
+                v = 1.0;
+            } else {
+                s = lower_bound_key(t.seg_cum, s0, s1, dkey(target));
+                if (s == s1) s = s1 - 1;
+                const double prev = s > s0 ? t.seg_cum[s - 1] : 0.0;
+                const double rr = target - prev;
+                const int64_t lo = t.leaf_off[s];
+                const int cnt = t.leaf_cnt[s];
+                int64_t j = lower_bound_key(t.leaf_cum, lo, lo + cnt, dkey(rr)) - lo;
+                if (j >= cnt) j = cnt - 1;
+                const double base = j ? t.leaf_cum[lo + j - 1] : 0.0;
+                const double va = j ? t.leaf_v[lo + j - 1] : -1.0;
+                const double fa = j ? t.leaf_f[lo + j - 1] : t.seg_f0[s];
+                const double vb = t.leaf_v[lo + j];
+                const double cb = t.leaf_cum[lo + j];
+                const double fb = t.leaf_f[lo + j];
+                const double dS = cb - base, dv = vb - va;
+                // initial guess: cubic Hermite of v(S) with slopes 1/f at the ends
+                double sig = dS > 0.0 ? (rr - base) / dS : 0.0;
+                sig = fmin(fmax(sig, 0.0), 1.0);
+                double vg = va + sig * dv;
+                const double fm = dS / dv;
+                if (fa > 0.1 * fm && fb > 0.1 * fm) {
+                    const double s2 = sig * sig, s3 = s2 * sig;
+                    const double h10 = s3 - 2.0 * s2 + sig, h11 = s3 - s2;
+                    const double h01 = 3.0 * s2 - 2.0 * s3;
+                    vg = va + h01 * dv + dS * (h10 / fa + h11 / fb);
+                    vg = fmin(fmax(vg, va), vb);
+                }
+                const double* seg = t.coef + b.coef_off[c] + (s - s0) * code_stride(code);
+                double r[MAX_COEF];
+                if constexpr (CODE >= 0)
+                    Eval<(CODE >= 0 ? CODE : 0)>::load_speed(seg, r);
+                else
+                    load_speed_dyn(code, seg, r);
+                double blo = va, bhi = vb;
+                v = vg;
+                const double stop = 1e-9 * dv;
+                for (int it = 0; it < NEWTON_MAXIT; ++it) {
+                    ++newton;
+                    const double h2 = 0.5 * (v - va);
+                    const double m2 = va + h2;
+                    double I = 0.0;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const double xk = h2 * gl8_x(k);
+                        I = fma(gl8_w(k), speed_of<CODE>(code, r, m2 - xk) + speed_of<CODE>(code, r, m2 + xk), I);
+                    }
+                    const double F = (base + I * h2) - rr;
+                    if (F == 0.0) break;
+                    if (F < 0.0)
+                        blo = v;
+                    else
+                        bhi = v;
+                    const double fv = speed_of<CODE>(code, r, v);
+                    double vn = v - F / fv;
+                    if (!(vn > blo && vn < bhi)) vn = 0.5 * (blo + bhi);
+                    const double step = fabs(vn - v);
+                    v = vn;
+                    if (step <= stop) break;
+                }
+            }
+        }
+        if (P.what == 2) {
+            double u;
+            if (s < 0) {
+                u = b.kind[c] == 0 ? 0.0 : b.knots[b.knot_off[c] + b.degree[c]];
+            } else {
+                // exact at both ends of the knot interval
+                const double t0 = t.seg_t0[s], t1 = t.seg_t1[s], hw = 0.5 * (t1 - t0);
+                u = v <= 0.0 ? fma(v + 1.0, hw, t0) : fma(v - 1.0, hw, t1);
+            }
+            P.out[i] = u;
+        } else {
+            double p3[3] = {0.0, 0.0, 0.0};
+            if (s >= 0) {
+                const double* seg = t.coef + b.coef_off[c] + (s - s0) * code_stride(code);
+                if constexpr (CODE >= 0)
+                    Eval<(CODE >= 0 ? CODE : 0)>::point(seg, v, p3);
+                else
+                    point_dyn(code, seg, v, p3);
+            }
+            for (int k = 0; k < P.pdim; ++k) P.out[i * P.pdim + k] = p3[k];
+        }
+    }
+    if (P.collect) {
+        for (int o = 16; o > 0; o >>= 1) newton += __shfl_xor_sync(0xffffffffu, newton, o);
+        if ((threadIdx.x & 31) == 0 && newton) atomicAdd(t.ctr + C_NEWTON, newton);
+    }
+}
+
+// ------------------------------------------------------------ FMA probe
+// Register-only throughput probe: 8 independent FMA chains per thread.
+template <typename T>
+__global__ void k_fma_probe(T* out, int iters, T seed)
+{
+    T a[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = seed + T(threadIdx.x + k);
+    const T m = T(0.999999), c = T(1e-7);
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) a[k] = fma(a[k], m, c);
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s += a[k];
+    if (s == T(-1.2345)) out[0] = s;  // never true; keeps the chains live
+}
+
+}  // namespace gcv

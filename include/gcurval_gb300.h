@@ -1,0 +1,213 @@
+/* gcurval_gb300 C ABI: adaptive arc length and arc-length sampling of
+ * parametric curves on one GB300 GPU (sm_103a).
+ *
+ * This is the drop-in boundary for gcurval's arc-length path.  Every entry
+ * point replaces one member of the reference's driver class
+ * gcurval::ArclengthCalculateCuda (gcurval/detail/cuda/arclength_calculate.h)
+ * or one of the sample plugins' constructors; the citation is given beside
+ * each declaration.  Plain pointers and sizes only: no CUDA or torch types
+ * (a stream is passed as void*).
+ *
+ * Curve kinds built into the library:
+ *   - ellipses  x = a cos t, y = b sin t, t in [0, 2 pi] (one knot interval),
+ *               optionally rotated by `rot` and moved to (cx, cy)
+ *               (samples/sample1_ellipse/ellipse.h);
+ *   - B-splines of degree 1..5 in 2D or 3D over their knot vector, one knot
+ *               interval per segment (samples/sample2_bspline/).
+ * User-defined curve functors go through the C++ header
+ * include/gcurval/arclength_calculate.h, which instantiates the same kernels
+ * on the user's plugin types.
+ *
+ * Errors: every entry point returns a gcv_status; gcv_last_error() gives a
+ * message for the calling thread.  The reference instead calls exit(-1) in
+ * debug builds and ignores errors under NDEBUG
+ * (gcurval/detail/cuda/util.h:14-34).
+ *
+ * Threading: a context is used by one host thread at a time.  All GPU work of
+ * a context runs on its stream (options.stream, default the legacy default
+ * stream), like the reference's single stream.
+ */
+#ifndef GCURVAL_GB300_H
+#define GCURVAL_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gcv_status {
+    GCV_OK = 0,
+    GCV_ERR_INVALID = 1,      /* bad argument or curve data */
+    GCV_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    GCV_ERR_OUT_OF_MEMORY = 3,
+    GCV_ERR_STATE = 4,        /* e.g. sampling before the table exists */
+    GCV_ERR_OVERFLOW = 5,     /* a fixed-capacity device structure overflowed */
+    GCV_ERR_TIMEOUT = 6,      /* a bounded device-side wait gave up */
+    GCV_ERR_NO_DEVICE = 7     /* no usable GPU / the kernels cannot run */
+} gcv_status;
+
+/* Mirrors gcurval::GcurvalEnum (gcurval/base/util.h:71-77): where a result
+ * lives and what it holds.  The numeric values match the reference enum. */
+typedef enum gcv_enum {
+    GCV_DEVICE = 0,        /* gcurvalDevice */
+    GCV_HOST = 1,          /* gcurvalHost */
+    GCV_RETURN_US = 2,     /* gcurvalReverseReturnUs */
+    GCV_RETURN_POINTS = 3  /* gcurvalReverseReturnPoints */
+} gcv_enum;
+
+typedef enum gcv_precision {
+    GCV_PLAIN_FP64 = 0,    /* every step in FP64 */
+    GCV_MIXED = 1          /* FP32 integrand and panels; FP64 prefix sum,
+                              error test near tolerance and final Newton step */
+} gcv_precision;
+
+typedef enum gcv_kind { GCV_KIND_ELLIPSE = 0, GCV_KIND_BSPLINE = 1 } gcv_kind;
+
+/* Run-time replacements of the reference's compile-time configuration
+ * (gcurval/config.h: GCURVAL_MAX_ERROR, GCURVAL_MAX_RECURSIVE_DEPTH). */
+typedef struct gcv_options {
+    double rtol;          /* relative tolerance on every knot interval's length
+                             (default 1e-10 for GCV_PLAIN_FP64, 1e-8 for GCV_MIXED) */
+    int max_depth;        /* maximum bisection depth below one knot interval (default 30) */
+    int precision;        /* gcv_precision */
+    void* stream;         /* cudaStream_t; NULL = legacy default stream */
+    int collect_stats;    /* nonzero: count panels and Newton steps (gcv_get_stats) */
+} gcv_options;
+
+typedef struct gcv_ctx gcv_ctx;
+
+/* Result of gcv_arclength_reverse; mirrors gcurval::ArclengthReverseResult
+ * (gcurval/base/structs.inl.h:66-77).  `data` holds n_points parameters u, or
+ * n_points points of point_dim doubles (x, y[, z]); it is device memory when
+ * store_where == GCV_DEVICE, else host memory.  Release it with
+ * gcv_free_result (the reference has no free helper and leaks it to the
+ * caller, gcurval/detail/cuda/arclength_calculate.h:462-499). */
+typedef struct gcv_result {
+    int64_t n_points;
+    int store_where;
+    int store_what;
+    int point_dim;
+    double* data;
+} gcv_result;
+
+/* Counters of the last table build / sampling call (filled when
+ * options.collect_stats is set; the timings always). */
+typedef struct gcv_stats {
+    int64_t n_curves;
+    int64_t n_segments;       /* knot intervals */
+    int64_t n_leaves;         /* accepted quadrature panels (table entries) */
+    int64_t n_panels;         /* panels evaluated by the length kernel */
+    int64_t n_deep_segments;  /* intervals that needed the deep (global-memory) path */
+    int64_t n_capped;         /* panels accepted at max_depth without meeting rtol */
+    int64_t n_samples;
+    int64_t n_newton;         /* Newton iterations of the sampling kernel */
+    double ms_setup, ms_length, ms_scan, ms_sample;  /* device time per phase */
+    int64_t n_launches;       /* kernels launched by the context so far */
+} gcv_stats;
+
+const char* gcv_status_string(gcv_status s);
+const char* gcv_last_error(void);
+int gcv_version(void);
+
+/* Fills *opt with the defaults for `precision`. */
+gcv_status gcv_default_options(gcv_options* opt, int precision);
+
+/* ---- construction ------------------------------------------------------ */
+
+/* Ellipses.  Replaces the ellipse sample's
+ * ArclengthCalculateGpu(int n_curve, Dt* a, Dt* b)
+ * (samples/sample1_ellipse/ellipse.h:121-129) over
+ * ArclengthCalculateCuda(int n_curve, int n_seg) (arclength_calculate.h:141-153).
+ * rot, cx, cy may be NULL (0).  where = GCV_HOST copies the arrays to the
+ * device; GCV_DEVICE uses the caller's device arrays, which must stay alive
+ * and unchanged for the life of the context (the reference's subclass fills
+ * d_curve with device pointers it owns, ellipse.h:121-135). */
+gcv_status gcv_create_ellipses(gcv_ctx** out, int n_curve, const double* a, const double* b,
+                               const double* rot, const double* cx, const double* cy, int where,
+                               const gcv_options* opt);
+
+/* B-splines of one degree and dimension in the reference sample's layout:
+ * knots_offset[n_curve + 1] (int32, prefix of knot counts), knot vectors back
+ * to back, control points back to back (dim doubles each; curve c's first
+ * control point is knots_offset[c] - (degree + 1) * c).  Replaces
+ * ArclengthCalculateGpu(int n_curve, int* knots_offset, Dt* knot_vector,
+ * Vector* ctrl_ptrs) (samples/sample2_bspline/arclength_calculate.h:505-518)
+ * with n_seg = knots_offset[n] - (2 degree + 1) n (:506). */
+gcv_status gcv_create_bsplines(gcv_ctx** out, int n_curve, int degree, int dim,
+                               const int* knots_offset, const double* knot_vector,
+                               const double* ctrl_pts, int where, const gcv_options* opt);
+
+/* A batch of uneven curves (any mix of ellipses and B-splines of degree 1..5,
+ * 2D/3D): per-curve kind/degree/dim, int64 offsets into one knot array and
+ * one control array (ellipses: knots {0, 2 pi}, control a, b, rot, cx, cy).
+ * No reference counterpart: the reference fixes kind and degree per
+ * template instantiation (gcurval/arclength_calculate.h:10-18). */
+gcv_status gcv_create_batch(gcv_ctx** out, int n_curve, const uint8_t* kind, const uint8_t* degree,
+                            const uint8_t* dim, const int64_t* knot_off, const double* knots,
+                            const int64_t* ctrl_off, const double* ctrl, int where,
+                            const gcv_options* opt);
+
+/* ~ArclengthCalculateCuda (arclength_calculate.h:168-183). */
+gcv_status gcv_destroy(gcv_ctx* ctx);
+
+/* Changes rtol / max_depth / precision / stream of an existing context; the
+ * next gcv_create_arclength_table uses them. */
+gcv_status gcv_set_options(gcv_ctx* ctx, const gcv_options* opt);
+
+/* ---- arc length ----------------------------------------------------------- */
+
+/* createArclengthTable (arclength_calculate.h:185-210): adaptive length of
+ * every knot interval, then the per-curve cumulative table.  Asynchronous on
+ * the context's stream except for one device-to-host read of the table size. */
+gcv_status gcv_create_arclength_table(gcv_ctx* ctx);
+
+/* getAllCurveArclengths (arclength_calculate.h:212-216): total length of every
+ * curve into out[n_curve] (host or device memory per `where`).  Unlike the
+ * reference, the caller provides the buffer instead of receiving new[]. */
+gcv_status gcv_get_all_curve_arclengths(gcv_ctx* ctx, double* out, int where);
+
+/* getArclength (arclength_calculate.h:218-222). */
+gcv_status gcv_get_arclength(gcv_ctx* ctx, int cid, double* out);
+
+/* arclengthReverse (arclength_calculate.h:224-231,408-505): n_ptrs_for_curves
+ * (n_curve ints) samples per curve at sample_position (sum of counts doubles;
+ * fractions of each curve's length when is_relative, else absolute lengths).
+ * Inputs are host memory, as in the reference.  The result is allocated by
+ * the library in `where` memory (GCV_DEVICE, the reference's default, or
+ * GCV_HOST) and holds parameters (GCV_RETURN_US) or points
+ * (GCV_RETURN_POINTS). */
+gcv_status gcv_arclength_reverse(gcv_ctx* ctx, const int* n_ptrs_for_curves,
+                                 const double* sample_position, int is_relative, int where,
+                                 int what, gcv_result* result);
+
+/* The same into caller-provided memory: counts and positions in `in_where`
+ * memory, output `out` (n points or n * point_dim doubles) in `out_where`
+ * memory.  No allocation for the result. */
+gcv_status gcv_arclength_reverse_into(gcv_ctx* ctx, const int* n_ptrs_for_curves,
+                                      const double* sample_position, int is_relative,
+                                      int in_where, int what, double* out, int out_where);
+
+gcv_status gcv_free_result(gcv_result* result);
+
+/* clearArclength (arclength_calculate.h:233-237): drops the cached lengths. */
+gcv_status gcv_clear_arclength(gcv_ctx* ctx);
+
+/* ---- introspection -------------------------------------------------------- */
+
+gcv_status gcv_synchronize(gcv_ctx* ctx);
+gcv_status gcv_get_stats(gcv_ctx* ctx, gcv_stats* out);
+/* n_curve, total knot intervals and point dimension of a context. */
+gcv_status gcv_get_shape(gcv_ctx* ctx, int64_t* n_curve, int64_t* n_segments, int* point_dim);
+
+/* Measures the current GPU's fused multiply-add throughput with a register-
+ * only kernel (which = 0: FP64, 1: FP32) in TFLOP/s (an FMA counts 2).  Used
+ * as the roofline denominator of the FP-pipe-bound kernels.  No reference
+ * counterpart. */
+gcv_status gcv_measure_fma_peak(int which, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GCURVAL_GB300_H */

@@ -350,7 +350,7 @@ int gcvref_ellipse_run(int n, const double* a, const double* b, const int* n_per
     return 0;
 }
 
-// Same for B-splines of one degree (2..5) and dimension (2, 3) in the
+// Same for B-splines of one degree (1..5) and dimension (2, 3) in the
 // reference's packed layout: knots_offset[n + 1], knot vectors back to back,
 // control points back to back (D doubles each).
 int gcvref_bspline_run(int n, int degree, int dim, const int* knots_offset, const double* knots,
@@ -361,8 +361,8 @@ int gcvref_bspline_run(int n, int degree, int dim, const int* knots_offset, cons
     if (degree == P && dim == D)                                                                   \
         return bspline_run<P, D>(n, knots_offset, knots, ctrl, n_per_curve, pos, is_relative, what, \
                                  out, lengths, nthreads);
-    GCVREF_CASE(2, 2) GCVREF_CASE(3, 2) GCVREF_CASE(4, 2) GCVREF_CASE(5, 2)
-    GCVREF_CASE(2, 3) GCVREF_CASE(3, 3) GCVREF_CASE(4, 3) GCVREF_CASE(5, 3)
+    GCVREF_CASE(1, 2) GCVREF_CASE(2, 2) GCVREF_CASE(3, 2) GCVREF_CASE(4, 2) GCVREF_CASE(5, 2)
+    GCVREF_CASE(1, 3) GCVREF_CASE(2, 3) GCVREF_CASE(3, 3) GCVREF_CASE(4, 3) GCVREF_CASE(5, 3)
 #undef GCVREF_CASE
     return -1;
 }

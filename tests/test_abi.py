@@ -1,0 +1,75 @@
+"""The C-ABI library builds for sm_103a, loads, exports every symbol the public
+header declares, and rejects bad input before touching a GPU."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import gcurval_gb300 as g
+from gcurval_gb300 import _lib, build
+
+
+def test_library_builds_and_exports_header_symbols():
+    path = build.build()
+    assert os.path.exists(path)
+    lib = g.load()
+    declared = _lib.declared_symbols()
+    assert len(declared) >= 15
+    for name in declared:
+        assert hasattr(lib, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\b(gcv_[a-z0-9_]+)\b", out))
+    assert set(declared) <= exported
+
+
+def test_build_targets_sm103a_only():
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_status_strings_and_defaults():
+    lib = g.load()
+    assert lib.gcv_status_string(0) == b"ok"
+    assert lib.gcv_status_string(7) == b"no usable CUDA device"
+    o = g.default_options(g.GCV_PLAIN_FP64)
+    assert o.rtol == 1e-10 and o.max_depth == 30 and o.precision == 0
+    m = g.default_options(g.GCV_MIXED)
+    assert m.rtol == 1e-8 and m.precision == 1
+
+
+def test_invalid_options_rejected_without_gpu():
+    lib = g.load()
+    o = g.default_options()
+    o.rtol = 0.0
+    h = ctypes.c_void_p()
+    a = np.ones(2)
+    st = lib.gcv_create_ellipses(ctypes.byref(h), 2, a.ctypes.data_as(ctypes.c_void_p),
+                                 a.ctypes.data_as(ctypes.c_void_p), None, None, None, g.GCV_HOST, ctypes.byref(o))
+    assert st == _lib.GCV_ERR_INVALID
+    assert b"rtol" in lib.gcv_last_error()
+    o = g.default_options()
+    o.max_depth = 99
+    st = lib.gcv_create_ellipses(ctypes.byref(h), 2, a.ctypes.data_as(ctypes.c_void_p),
+                                 a.ctypes.data_as(ctypes.c_void_p), None, None, None, g.GCV_HOST, ctypes.byref(o))
+    assert st == _lib.GCV_ERR_INVALID
+
+
+def test_bad_degree_rejected_without_gpu():
+    lib = g.load()
+    h = ctypes.c_void_p()
+    ko = np.array([0, 8], np.int32)
+    kv = np.zeros(8)
+    cp = np.zeros(8)
+    st = lib.gcv_create_bsplines(ctypes.byref(h), 1, 7, 2, ko.ctypes.data_as(ctypes.c_void_p),
+                                 kv.ctypes.data_as(ctypes.c_void_p), cp.ctypes.data_as(ctypes.c_void_p), g.GCV_HOST,
+                                 None)
+    assert st == _lib.GCV_ERR_INVALID
+
+
+def test_null_handles_rejected():
+    lib = g.load()
+    assert lib.gcv_destroy(None) == _lib.GCV_ERR_INVALID
+    assert lib.gcv_create_arclength_table(None) == _lib.GCV_ERR_INVALID
+    assert lib.gcv_free_result(None) == _lib.GCV_ERR_INVALID
