@@ -64,12 +64,16 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-sample-curves", type=int, default=0, help="curves in the CPU-baseline sample (0: auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-curves", type=int, default=0, help="override the workload's curve count (profiling runs)")
     return ap.parse_args()
 
 
-def make_batch(workload: str, seed: int):
+def make_batch(workload: str, seed: int, n_curves: int = 0):
     from gcurval_gb300 import datasets as ds
     kw, _ = WORKLOADS[workload]
+    kw = dict(kw)
+    if n_curves:
+        kw["n"] = n_curves
     gen = ds.WORKLOADS[workload]
     b = gen(seed=seed, **kw)
     b.sample_positions()
@@ -195,7 +199,7 @@ def main():
     from gcurval_gb300 import _lib
 
     precision = g.GCV_MIXED if args.precision == "mixed" else g.GCV_PLAIN_FP64
-    batch = make_batch(args.workload, seed=rank)
+    batch = make_batch(args.workload, seed=rank, n_curves=args.n_curves)
     pos = batch.positions
     n_curves, n_samples = batch.n_curve, batch.total_samples
 
@@ -244,7 +248,9 @@ def main():
         t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    launches = calc.stats()["n_launches"] - launches0
+    st1 = calc.stats()
+    launches = st1["n_launches"] - launches0
+    leaves = st1["n_leaves"]
     ms_per_step = total_ms / args.steps
     value = world * n_curves / (ms_per_step * 1e-3)
     samples_per_s = world * n_samples / (ms_per_step * 1e-3)
@@ -288,6 +294,10 @@ def main():
                 "frac": round(bytes_alg / (ms * 1e-3) / 1e9 / hbm_peak, 4) if hbm_peak else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
         "phases_ms": {"length": round(ms_l, 4), "sample": round(ms_s, 4)},
+        "work_per_step": {"panels": float(np.mean(n_panels)), "newton_iterations": float(np.mean(n_newton)),
+                          "leaves": int(leaves), "segments": int(batch.n_segments.sum()),
+                          "length_tflops": round(len_flops / (ms_l * 1e-3) / 1e12, 4),
+                          "sample_tflops": round(samp_flops / (ms_s * 1e-3) / 1e12, 4)},
         "fp32_peak_tflops": round(fp32_peak, 2),
     }
     calc.close()
@@ -351,7 +361,7 @@ def main():
 
 def reference_arm(args):
     nthreads = os.cpu_count() or 1
-    batch = make_batch(args.workload, seed=0)
+    batch = make_batch(args.workload, seed=0, n_curves=args.n_curves)
     sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch))
     times, kind = [], None
     for i in range(max(args.warmup, 3) + args.steps):

@@ -247,6 +247,7 @@ class ArclengthCalculateGpu:
                          what=GCV_RETURN_US) -> ArclengthReverseResult:
         n = np.ascontiguousarray(n_ptrs_for_curves, np.int32)
         pos = np.ascontiguousarray(sample_position, np.float64)
+        self._check_counts(n, pos.shape[0])
         r = Result()
         check(self._lib.gcv_arclength_reverse(self._h, _ptr(n), _ptr(pos), int(bool(is_relative)), int(where),
                                               int(what), ctypes.byref(r)))
@@ -259,6 +260,11 @@ class ArclengthCalculateGpu:
         if _is_device(n) != in_dev:
             raise ValueError("counts and positions must live in the same memory")
         pos = sample_position if in_dev else np.ascontiguousarray(sample_position, np.float64)
+        total = self._check_counts(n, int(pos.shape[0]))
+        width = 1 if what == GCV_RETURN_US else self.point_dim
+        n_out = int(out.numel()) if hasattr(out, "numel") else int(out.size)
+        if n_out < total * width:
+            raise ValueError(f"output holds {n_out} values, {total * width} needed")
         check(self._lib.gcv_arclength_reverse_into(self._h, _ptr(n), _ptr(pos), int(bool(is_relative)),
                                                    GCV_DEVICE if in_dev else GCV_HOST, int(what), _ptr(out),
                                                    GCV_DEVICE if _is_device(out) else GCV_HOST))
@@ -266,6 +272,16 @@ class ArclengthCalculateGpu:
 
     def clearArclength(self):
         check(self._lib.gcv_clear_arclength(self._h))
+
+    def _check_counts(self, n, n_positions: int) -> int:
+        """The C ABI reads n_curve counts and their sum of positions through raw
+        pointers, as the reference does; check the sizes before handing them over."""
+        if tuple(n.shape) != (self.n_curve,):
+            raise ValueError(f"{n.shape[0] if len(n.shape) else 0} sample counts for {self.n_curve} curves")
+        total = int(n.sum())
+        if total != n_positions:
+            raise ValueError(f"sample counts add up to {total}, {n_positions} positions given")
+        return total
 
     # ------------------------------------------------------------- extras
     def synchronize(self):

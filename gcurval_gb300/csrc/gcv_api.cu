@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "gcv_kernels.cuh"
+#include "gcv_length.cuh"
 #include "gcv_mixed.cuh"
 
 using namespace gcv;
@@ -443,8 +444,9 @@ gcv_status launch_length(gcv_ctx* c, const LengthParams& P)
     default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, -1>, LK_THREADS, 0); break;
     }
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
-    occ = std::max(1, std::min(occ, 16));
-    int64_t want = (P.n_items + LK_HALVES - 1) / LK_HALVES;
+    occ = std::max(1, std::min(occ, 32));
+    // persistent: fill the GPU, but no more lanes than there are intervals
+    int64_t want = (P.n_items + LK_THREADS - 1) / LK_THREADS;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * occ, want));
     switch (c->code) {
     case CODE_ELLIPSE: k_length<MODE, CODE_ELLIPSE><<<grid, LK_THREADS, 0, c->stream>>>(P); break;

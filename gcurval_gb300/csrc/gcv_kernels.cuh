@@ -144,229 +144,6 @@ __global__ void k_seg_curve(Batch b, int* seg_curve)
     }
 }
 
-// ------------------------------------------------------ adaptive length
-// Persistent half-warp workers.  A half-warp (16 lanes) owns one segment at a
-// time and refines it depth-first: each iteration evaluates one panel with
-// the 15-node Kronrod rule (lanes 0..14) plus the panel's right end (lane 15),
-// reduces K15 and G7 with an xor butterfly, and either accepts the panel
-// (|K15 - G7| within the panel's share of rtol * length) or splits it,
-// pushing the right half on a shared-memory stack.  Accepted panels leave in
-// parameter order and are staged in shared memory, then copied to the leaf
-// pool at an atomically reserved offset.  Segments with more than LCAP leaves
-// go to a deep list and are redone by the MODE 1 (count) / MODE 2 (write)
-// passes, which write straight to the pool.
-constexpr int LK_THREADS = 128;
-constexpr int LK_HALVES = LK_THREADS / 16;
-constexpr int STACK_CAP = 40;
-constexpr int LCAP = 48;
-constexpr int LK_CHUNK = 4;
-constexpr long long PANEL_BUDGET = 1ll << 22;
-constexpr int MAX_DEPTH_LIMIT = STACK_CAP - 2;
-
-struct LengthParams {
-    Batch b;
-    Table t;
-    double rtol;
-    int max_depth;
-    int collect;
-    const int* list;  // segments to process (deep passes); NULL: all segments
-    int64_t n_items;
-};
-
-template <int MODE, int CODE>
-__global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
-{
-    __shared__ double st_v[LK_HALVES][STACK_CAP];
-    __shared__ int st_d[LK_HALVES][STACK_CAP];
-    __shared__ double lf_v[MODE == 0 ? LK_HALVES : 1][MODE == 0 ? LCAP : 1];
-    __shared__ double lf_c[MODE == 0 ? LK_HALVES : 1][MODE == 0 ? LCAP : 1];
-    __shared__ double lf_f[MODE == 0 ? LK_HALVES : 1][MODE == 0 ? LCAP : 1];
-
-    const Batch& b = P.b;
-    const Table& t = P.t;
-    const int lane = threadIdx.x & 31;
-    const int hl = lane & 15;
-    const int half = threadIdx.x >> 4;
-    const unsigned hmask = (lane < 16) ? 0x0000FFFFu : 0xFFFF0000u;
-    const int hbase = lane & 16;
-    double xn, wk, wg;
-    gk_lane(hl, xn, wk, wg);
-    const double eps50 = 50.0 * 2.220446049250313e-16;
-
-    int64_t next = 0, end = 0;
-    unsigned long long my_panels = 0, my_capped = 0, my_nonfinite = 0;
-
-    for (;;) {
-        if (next == end) {
-            unsigned long long base = 0;
-            if (hl == 0) base = atomicAdd(t.ctr + C_WORK, (unsigned long long)LK_CHUNK);
-            base = __shfl_sync(hmask, base, hbase);
-            if ((int64_t)base >= P.n_items) break;
-            next = (int64_t)base;
-            end = min((int64_t)base + LK_CHUNK, P.n_items);
-        }
-        const int64_t item = next++;
-        const int64_t s = P.list ? (int64_t)P.list[item] : item;
-        const int64_t c = b.seg_curve[s];
-        const int code = CODE >= 0 ? CODE : curve_code(b, c);
-        const double* seg = t.coef + b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
-        double r[MAX_COEF];
-        if constexpr (CODE >= 0)
-            Eval<(CODE >= 0 ? CODE : 0)>::load_speed(seg, r);
-        else
-            load_speed_dyn(code, seg, r);
-
-        int64_t pool = 0;
-        if (MODE == 2) {
-            unsigned long long o = 0;
-            if (hl == 0) o = atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)t.leaf_cnt[s]);
-            pool = (int64_t)__shfl_sync(hmask, o, hbase);
-            if (pool + t.leaf_cnt[s] > t.leaf_cap) {
-                if (hl == 0) raise_err(t, ERR_POOL);
-                continue;
-            }
-        }
-
-        if (t.seg_t1[s] == t.seg_t0[s]) {  // zero-width knot interval: one empty leaf
-            if (MODE == 0) {
-                unsigned long long o = 0;
-                if (hl == 0) o = atomicAdd(t.ctr + C_LEAF_TOP, 1ull);
-                o = __shfl_sync(hmask, o, hbase);
-                if (hl == 0) {
-                    if ((int64_t)o < t.leaf_cap) {
-                        t.leaf_v[o] = 1.0;
-                        t.leaf_cum[o] = 0.0;
-                        t.leaf_f[o] = 0.0;
-                    } else {
-                        raise_err(t, ERR_POOL);
-                    }
-                    t.seg_len[s] = 0.0;
-                    t.leaf_off[s] = (int64_t)o;
-                    t.leaf_cnt[s] = 1;
-                }
-            } else if (hl == 0) {
-                if (MODE == 1) t.leaf_cnt[s] = 1;
-                if (MODE == 2) {
-                    t.leaf_v[pool] = 1.0;
-                    t.leaf_cum[pool] = 0.0;
-                    t.leaf_f[pool] = 0.0;
-                    t.seg_len[s] = 0.0;
-                    t.leaf_off[s] = pool;
-                }
-            }
-            continue;
-        }
-
-        double v_lo = -1.0, cum = 0.0, tol_unit = 0.0;
-        int depth = 0, sp = 0, nleaf = 0;
-        long long panels = 0;
-        bool overflow = false;
-        for (;;) {
-            const double hw = pow2_neg(depth);
-            const double mid = v_lo + hw;
-            const double v = fma(hw, xn, mid);
-            double f;
-            if constexpr (CODE >= 0)
-                f = Eval<(CODE >= 0 ? CODE : 0)>::speed(r, v);
-            else
-                f = speed_dyn(code, r, v);
-            const double K = half_sum(f * wk, hmask) * hw;
-            const double G = half_sum(f * wg, hmask) * hw;
-            const double fend = __shfl_sync(hmask, f, hbase + 15);
-            if (depth == 0) tol_unit = P.rtol * fabs(K);
-            const double err = fabs(K - G);
-            ++panels;
-            const bool finite = isfinite(K) && isfinite(G);
-            const bool at_cap = depth >= P.max_depth || panels >= PANEL_BUDGET;
-            const bool ok = err <= fmax(tol_unit * hw, eps50 * fabs(K));
-            if (ok || at_cap || !finite) {
-                if (!ok && finite) ++my_capped;
-                if (!finite) ++my_nonfinite;
-                cum += K;
-                const double vr = v_lo + 2.0 * hw;
-                if (MODE == 0) {
-                    if (nleaf < LCAP) {
-                        if (hl == 0) {
-                            lf_v[half][nleaf] = vr;
-                            lf_c[half][nleaf] = cum;
-                            lf_f[half][nleaf] = fend;
-                        }
-                    } else {
-                        overflow = true;
-                        break;
-                    }
-                } else if (MODE == 2) {
-                    if (hl == 0) {
-                        t.leaf_v[pool + nleaf] = vr;
-                        t.leaf_cum[pool + nleaf] = cum;
-                        t.leaf_f[pool + nleaf] = fend;
-                    }
-                }
-                ++nleaf;
-                if (sp == 0) break;
-                --sp;
-                v_lo = st_v[half][sp];
-                depth = st_d[half][sp];
-            } else {
-                if (hl == 0) {
-                    st_v[half][sp] = mid;
-                    st_d[half][sp] = depth + 1;
-                }
-                __syncwarp(hmask);
-                ++sp;
-                ++depth;
-            }
-        }
-        my_panels += panels;
-
-        if (MODE == 0) {
-            if (overflow) {
-                unsigned long long o = 0;
-                if (hl == 0) o = atomicAdd(t.ctr + C_DEEP, 1ull);
-                o = __shfl_sync(hmask, o, hbase);
-                if (hl == 0) {
-                    if ((int64_t)o < t.deep_cap)
-                        t.deep_list[o] = int(s);
-                    else
-                        raise_err(t, ERR_DEEP_LIST);
-                }
-                continue;
-            }
-            __syncwarp(hmask);
-            unsigned long long o = 0;
-            if (hl == 0) o = atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)nleaf);
-            o = __shfl_sync(hmask, o, hbase);
-            if ((int64_t)o + nleaf <= t.leaf_cap) {
-                for (int i = hl; i < nleaf; i += 16) {
-                    t.leaf_v[o + i] = lf_v[half][i];
-                    t.leaf_cum[o + i] = lf_c[half][i];
-                    t.leaf_f[o + i] = lf_f[half][i];
-                }
-            } else if (hl == 0) {
-                raise_err(t, ERR_POOL);
-            }
-            if (hl == 0) {
-                t.seg_len[s] = cum;
-                t.leaf_off[s] = (int64_t)o;
-                t.leaf_cnt[s] = nleaf;
-            }
-            __syncwarp(hmask);
-        } else if (MODE == 1) {
-            if (hl == 0) t.leaf_cnt[s] = nleaf;
-        } else {
-            if (hl == 0) {
-                t.seg_len[s] = cum;
-                t.leaf_off[s] = pool;
-            }
-        }
-    }
-    if (hl == 0 && (P.collect || my_capped || my_nonfinite)) {
-        if (P.collect) atomicAdd(t.ctr + C_PANELS, my_panels);
-        if (my_capped) atomicAdd(t.ctr + C_CAPPED, my_capped);
-        if (my_nonfinite) atomicAdd(t.ctr + C_NONFINITE, my_nonfinite);
-    }
-}
-
 // ------------------------------------------------- compensated scan
 // Single-pass segmented inclusive scan of segment lengths (segments of one
 // curve are contiguous; a curve's first segment starts a new sum) with
@@ -615,29 +392,39 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) k_sample(SampleParams P)
                     load_speed_dyn(code, seg, r);
                 double blo = va, bhi = vb;
                 v = vg;
-                const double stop = 1e-9 * dv;
+                // a step below 1e-7 of the leaf leaves an error of order
+                // (f'/f) * step^2: below 1e-14 of the leaf
+                const double stop = 1e-7 * dv;
                 for (int it = 0; it < NEWTON_MAXIT; ++it) {
                     ++newton;
-                    const double h2 = 0.5 * (v - va);
-                    const double m2 = va + h2;
+                    // integrate over the shorter side of v: S(v) = S(va) + GL8(va, v)
+                    // or S(vb) - GL8(v, vb); at most half a leaf, where GL8 is far
+                    // more accurate than the leaf's own G7 error estimate
+                    const bool from_left = (v - va) <= (vb - v);
+                    const double a0 = from_left ? va : v, a1 = from_left ? v : vb;
+                    const double h2 = 0.5 * (a1 - a0);
+                    const double m2 = a0 + h2;
                     double I = 0.0;
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {
                         const double xk = h2 * gl8_x(k);
                         I = fma(gl8_w(k), speed_of<CODE>(code, r, m2 - xk) + speed_of<CODE>(code, r, m2 + xk), I);
                     }
-                    const double F = (base + I * h2) - rr;
+                    const double F = (from_left ? base + I * h2 : cb - I * h2) - rr;
                     if (F == 0.0) break;
                     if (F < 0.0)
                         blo = v;
                     else
                         bhi = v;
                     const double fv = speed_of<CODE>(code, r, v);
-                    double vn = v - F / fv;
-                    if (!(vn > blo && vn < bhi)) vn = 0.5 * (blo + bhi);
-                    const double step = fabs(vn - v);
+                    const double dn = F / fv;
+                    if (fabs(dn) <= stop) {  // converged: the next step would be below 1e-18 of the leaf
+                        v = fmin(fmax(v - dn, va), vb);
+                        break;
+                    }
+                    double vn = v - dn;
+                    if (!(vn > blo && vn < bhi)) vn = 0.5 * (blo + bhi);  // safeguard (also NaN)
                     v = vn;
-                    if (step <= stop) break;
                 }
             }
         }

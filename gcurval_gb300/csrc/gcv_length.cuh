@@ -1,0 +1,271 @@
+// Adaptive length of every knot interval (FP64): persistent workers, one
+// lane per knot interval.
+//
+// Each lane owns one segment at a time and refines it depth-first over the
+// dyadic panels of v in [-1, 1].  A panel is named by (k, depth): it spans
+// [-1 + k 2^(1-depth), -1 + (k+1) 2^(1-depth)], so the depth-first walk needs
+// no stack: splitting goes to (2k, depth+1); after accepting a panel the next
+// one is (k+1) with its trailing zero bits shifted out (climbing out of
+// finished right children), and the walk ends when it climbs back to depth 0.
+// Each panel is one 15-node Kronrod rule with its embedded 7-node Gauss rule
+// plus the speed at the panel's right end, evaluated serially by the lane:
+// accepted when |K15 - G7| is within the panel's share (half width) of
+// rtol * |K15 of the whole interval|, or at max_depth / the panel budget.
+// Accepted panels ("leaves") leave in parameter order; up to LCAP of them
+// are staged in shared memory and copied to the leaf pool at an offset
+// reserved by one atomic per warp.  Intervals with more leaves go to a deep
+// list and are redone by the MODE 1 (count) and MODE 2 (write) passes, which
+// write straight to the pool.
+//
+// This replaces the reference's breadth-first bisection (one GL3 task per
+// thread, one launch and one host round trip per level,
+// gcurval/detail/cuda/kernel/bfs.inl.cuh:9-125 driven from
+// gcurval/detail/cuda/arclength_calculate.h:259-323).
+#pragma once
+
+#include "gcv_kernels.cuh"
+
+namespace gcv {
+
+constexpr int LK_THREADS = 64;
+constexpr int LCAP = 16;
+constexpr long long PANEL_BUDGET = 1ll << 22;
+constexpr int MAX_DEPTH_LIMIT = 48;
+
+struct LengthParams {
+    Batch b;
+    Table t;
+    double rtol;
+    int max_depth;
+    int collect;
+    const int* list;  // segments to process (deep passes); NULL: all segments
+    int64_t n_items;
+};
+
+// K15, G7 and the right-end speed of panel [vlo, vlo + 2 hw].
+template <int CODE>
+__device__ __forceinline__ void panel_k15(const double* r, double vlo, double hw, double& K, double& G,
+                                          double& fend)
+{
+    const double mid = vlo + hw;
+    const double fc = Eval<CODE>::speed(r, mid);
+    double k = gk_wk(7) * fc;
+    double g = gk_wg(7) * fc;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        const double dx = hw * gk_x(i);
+        const double s = Eval<CODE>::speed(r, mid - dx) + Eval<CODE>::speed(r, mid + dx);
+        k = fma(gk_wk(i), s, k);
+        if (i & 1) g = fma(gk_wg(i), s, g);
+    }
+    fend = Eval<CODE>::speed(r, vlo + 2.0 * hw);
+    K = k * hw;
+    G = g * hw;
+}
+
+__device__ __forceinline__ void panel_dyn(int code, const double* r, double vlo, double hw, double& K, double& G,
+                                          double& fend)
+{
+    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: panel_k15<C>(r, vlo, hw, K, G, fend); break;
+        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+    default: K = G = fend = 0.0; break;
+    }
+}
+
+__device__ __forceinline__ int warp_incl_scan(int x, int lane)
+{
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= d) x += y;
+    }
+    return x;
+}
+
+template <int MODE, int CODE>
+__global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
+{
+    __shared__ double lf_v[MODE == 0 ? LCAP : 1][LK_THREADS];
+    __shared__ double lf_c[MODE == 0 ? LCAP : 1][LK_THREADS];
+    __shared__ double lf_f[MODE == 0 ? LCAP : 1][LK_THREADS];
+
+    const Batch& b = P.b;
+    const Table& t = P.t;
+    const int lane = threadIdx.x & 31;
+    const int tid = threadIdx.x;
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const double eps50 = 50.0 * 2.220446049250313e-16;
+
+    bool active = false, exhausted = false;
+    int64_t s = 0, pool = 0;
+    int code = CODE >= 0 ? CODE : 0;
+    double r[MAX_COEF];
+    unsigned long long k = 0;
+    int depth = 0, nleaf = 0;
+    double cum = 0.0, tol_unit = 0.0;
+    long long panels = 0;
+    unsigned long long my_panels = 0, my_capped = 0, my_nonfinite = 0;
+
+    for (;;) {
+        bool fin = false, ovf = false;
+        // ---- refill idle lanes with one atomic per warp
+        const bool need = !active && !exhausted;
+        const unsigned m = __ballot_sync(FULL, need);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(t.ctr + C_WORK, (unsigned long long)__popc(m));
+            base = __shfl_sync(FULL, base, leader);
+            if (need) {
+                const int64_t item = (int64_t)base + __popc(m & lt_mask);
+                if (item >= P.n_items) {
+                    exhausted = true;
+                } else {
+                    s = P.list ? (int64_t)P.list[item] : item;
+                    const int64_t c = b.seg_curve[s];
+                    if (CODE < 0) code = curve_code(b, c);
+                    const double* seg = t.coef + b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
+                    if constexpr (CODE >= 0)
+                        Eval<(CODE >= 0 ? CODE : 0)>::load_speed(seg, r);
+                    else
+                        load_speed_dyn(code, seg, r);
+                    k = 0;
+                    depth = 0;
+                    nleaf = 0;
+                    cum = 0.0;
+                    panels = 0;
+                    if (MODE == 2) {
+                        pool = (int64_t)atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)t.leaf_cnt[s]);
+                        if (pool + t.leaf_cnt[s] > t.leaf_cap) {
+                            raise_err(t, ERR_POOL);
+                            pool = -1;
+                        }
+                    }
+                    if (t.seg_t1[s] == t.seg_t0[s]) {  // zero-width knot interval: one empty leaf
+                        if (MODE == 0) {
+                            lf_v[0][tid] = 1.0;
+                            lf_c[0][tid] = 0.0;
+                            lf_f[0][tid] = 0.0;
+                        } else if (MODE == 2 && pool >= 0) {
+                            t.leaf_v[pool] = 1.0;
+                            t.leaf_cum[pool] = 0.0;
+                            t.leaf_f[pool] = 0.0;
+                        }
+                        nleaf = 1;
+                        fin = true;
+                    } else if (MODE != 2 || pool >= 0) {
+                        active = true;
+                    }
+                }
+            }
+        }
+        // ---- one panel per active lane
+        if (active) {
+            const double hw = pow2_neg(depth);
+            const double vlo = fma(__ull2double_rn(k), 2.0 * hw, -1.0);
+            double K, G, fend;
+            if constexpr (CODE >= 0)
+                panel_k15<(CODE >= 0 ? CODE : 0)>(r, vlo, hw, K, G, fend);
+            else
+                panel_dyn(code, r, vlo, hw, K, G, fend);
+            if (depth == 0) tol_unit = P.rtol * fabs(K);
+            ++panels;
+            const double err = fabs(K - G);
+            const bool finite = isfinite(K) && isfinite(G);
+            const bool at_cap = depth >= P.max_depth || panels >= PANEL_BUDGET;
+            const bool ok = err <= fmax(tol_unit * hw, eps50 * fabs(K));
+            if (ok || at_cap || !finite) {
+                if (!ok && finite) ++my_capped;
+                if (!finite) ++my_nonfinite;
+                cum += K;
+                const double vr = vlo + 2.0 * hw;
+                if (MODE == 0) {
+                    if (nleaf < LCAP) {
+                        lf_v[nleaf][tid] = vr;
+                        lf_c[nleaf][tid] = cum;
+                        lf_f[nleaf][tid] = fend;
+                    } else {
+                        ovf = true;
+                    }
+                } else if (MODE == 2) {
+                    t.leaf_v[pool + nleaf] = vr;
+                    t.leaf_cum[pool + nleaf] = cum;
+                    t.leaf_f[pool + nleaf] = fend;
+                }
+                ++nleaf;
+                ++k;
+                const int tz = __ffsll((long long)k) - 1;
+                k >>= tz;
+                depth -= tz;
+                if (ovf) {
+                    active = false;
+                } else if (depth == 0) {
+                    active = false;
+                    fin = true;
+                }
+            } else {
+                k <<= 1;
+                ++depth;
+            }
+            if (!active) my_panels += (unsigned long long)panels;
+        }
+        // ---- finished segments: outputs (leaf-pool offsets reserved per warp)
+        if (MODE == 0) {
+            const unsigned fm = __ballot_sync(FULL, fin);
+            if (fm) {
+                const int x = fin ? nleaf : 0;
+                const int incl = warp_incl_scan(x, lane);
+                const int total = __shfl_sync(FULL, incl, 31);
+                unsigned long long base = 0;
+                if (lane == 0) base = atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)total);
+                base = __shfl_sync(FULL, base, 0);
+                if (fin) {
+                    const int64_t off = (int64_t)base + incl - x;
+                    if (off + nleaf <= t.leaf_cap) {
+                        for (int i = 0; i < nleaf; ++i) {
+                            t.leaf_v[off + i] = lf_v[i][tid];
+                            t.leaf_cum[off + i] = lf_c[i][tid];
+                            t.leaf_f[off + i] = lf_f[i][tid];
+                        }
+                    } else {
+                        raise_err(t, ERR_POOL);
+                    }
+                    t.seg_len[s] = nleaf == 1 && t.seg_t1[s] == t.seg_t0[s] ? 0.0 : cum;
+                    t.leaf_off[s] = off;
+                    t.leaf_cnt[s] = nleaf;
+                }
+            }
+            if (ovf) {
+                const unsigned long long o = atomicAdd(t.ctr + C_DEEP, 1ull);
+                if ((int64_t)o < t.deep_cap)
+                    t.deep_list[o] = int(s);
+                else
+                    raise_err(t, ERR_DEEP_LIST);
+            }
+        } else if (fin) {
+            if (MODE == 1) t.leaf_cnt[s] = nleaf;
+            if (MODE == 2) {
+                t.seg_len[s] = t.seg_t1[s] == t.seg_t0[s] ? 0.0 : cum;
+                t.leaf_off[s] = pool;
+            }
+        }
+        if (__all_sync(FULL, exhausted && !active)) break;
+    }
+    // ---- statistics
+    for (int o = 16; o > 0; o >>= 1) {
+        my_panels += __shfl_xor_sync(FULL, my_panels, o);
+        my_capped += __shfl_xor_sync(FULL, my_capped, o);
+        my_nonfinite += __shfl_xor_sync(FULL, my_nonfinite, o);
+    }
+    if (lane == 0) {
+        if (P.collect && my_panels) atomicAdd(t.ctr + C_PANELS, my_panels);
+        if (my_capped) atomicAdd(t.ctr + C_CAPPED, my_capped);
+        if (my_nonfinite) atomicAdd(t.ctr + C_NONFINITE, my_nonfinite);
+    }
+}
+
+}  // namespace gcv

@@ -28,10 +28,12 @@
  *   ellipse_*()      point / derv_o1, samples/sample1_ellipse/ellipse.h:5-15
  *                    (plus rotation and centre for points, which leave |C'|
  *                    unchanged)
- * One deliberate difference: the reference starts the first table interval
+ * Two deliberate differences: the reference starts the first table interval
  * at u = 0 (cpu/arclength_calculate.h:200); here it starts at the curve's
- * first parameter value.  Every curve generated by this project starts at 0,
- * where both agree.
+ * first parameter value (every curve generated by this project starts at 0,
+ * where both agree).  And a zero-width knot span (a repeated knot) adds 0 to
+ * the length, where the reference's de Boor divides 0 by 0 and returns NaN
+ * for the whole curve (see build_curve).
  */
 #define _GNU_SOURCE
 #include "gcv_oracle.h"
@@ -241,6 +243,14 @@ static void build_curve(gcvo_table* t, int c, uint64_t* evals)
     for (int segid = 0; segid < nseg; segid++) {
         pack_t pk = make_pack(b, c, segid, evals);
         const double sb = pk.kv[pk.span], se = pk.kv[pk.span + 1];
+        if (se == sb) {
+            /* Zero-width knot span (repeated knot).  The reference evaluates
+             * de Boor here, divides 0 by 0 and turns the whole curve's length
+             * into NaN; the span's length is 0, so it contributes 0 and one
+             * table entry, as a guarded reference would. */
+            tab_push(tab, se, acc_curve + (0.0 - residual), segid);
+            continue;
+        }
         const double parent = gl3(&pk, sb, se);
         const int64_t store_begin = tab->n;
         const double acc_seg = seg_recursive(t, &pk, sb, se, parent, 0, 0.0, segid, tab);

@@ -115,9 +115,19 @@ class Oracle:
         d = np.where(self.batch.kind == 0, 2, self.batch.dim)
         return int(d[0]) if d.size and np.all(d == d[0]) else 3
 
-    def reverse(self, n_per_curve, positions, is_relative=True, what=0) -> np.ndarray:
+    def _counts(self, n_per_curve, values) -> np.ndarray:
+        """Sample counts checked against the table's curve count and the value array
+        (the C side trusts both sizes)."""
         n = np.ascontiguousarray(n_per_curve, np.int32)
+        if n.shape != (self.batch.n_curve,):
+            raise ValueError(f"{n.shape[0] if n.ndim else 0} sample counts for {self.batch.n_curve} curves")
+        if np.any(n < 0) or int(n.astype(np.int64).sum()) != values.shape[0]:
+            raise ValueError("sample counts do not match the number of values")
+        return n
+
+    def reverse(self, n_per_curve, positions, is_relative=True, what=0) -> np.ndarray:
         pos = np.ascontiguousarray(positions, np.float64)
+        n = self._counts(n_per_curve, pos)
         width = 1 if what == 0 else self.point_dim()
         out = np.zeros(int(n.astype(np.int64).sum()) * width)
         self.lib.gcvo_reverse(self.h, _ptr(n), _ptr(pos), int(bool(is_relative)), int(what), _ptr(out),
@@ -125,16 +135,20 @@ class Oracle:
         return out if what == 0 else out.reshape(-1, width)
 
     def s_at(self, n_per_curve, u) -> np.ndarray:
-        n = np.ascontiguousarray(n_per_curve, np.int32)
         u = np.ascontiguousarray(u, np.float64)
+        n = self._counts(n_per_curve, u)
         out = np.zeros(u.shape[0])
         self.lib.gcvo_s_at_many(self.h, _ptr(n), _ptr(u), _ptr(out), self.nthreads)
         return out
 
     def speed(self, cid: int, u: float) -> float:
+        if not 0 <= cid < self.batch.n_curve:
+            raise IndexError(cid)
         return self.lib.gcvo_speed(ctypes.byref(self._b), cid, u)
 
     def point(self, cid: int, u: float) -> np.ndarray:
+        if not 0 <= cid < self.batch.n_curve:
+            raise IndexError(cid)
         out = np.zeros(3)
         self.lib.gcvo_point(ctypes.byref(self._b), cid, u, _ptr(out))
         return out
@@ -146,6 +160,8 @@ class Oracle:
         return int(self.lib.gcvo_evals(self.h))
 
     def curve_table(self, cid: int):
+        if not 0 <= cid < self.batch.n_curve:
+            raise IndexError(cid)
         u = ctypes.POINTER(ctypes.c_double)()
         al = ctypes.POINTER(ctypes.c_double)()
         sg = ctypes.POINTER(ctypes.c_int)()

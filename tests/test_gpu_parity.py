@@ -186,7 +186,10 @@ def test_repeated_knots_and_degenerate_curves(gpu_lib):
     pos = np.r_[np.linspace(0, 1, 9), np.linspace(0, 1, 9)]
     u = calc.arclengthReverse([9, 9], pos, True, g.GCV_HOST).us
     assert np.all(np.isfinite(u))
-    assert np.max(sample_errors(o, b.subset([0]), u[:9], pos[:9], o.lengths()[:1])) <= POS_RTOL
+    np.testing.assert_array_equal(u[9:], 0.0)  # a zero-length curve samples at its start
+    sub = b.subset([0])
+    o0 = Oracle(sub)
+    assert np.max(sample_errors(o0, sub, u[:9], pos[:9], o0.lengths())) <= POS_RTOL
     assert np.all(np.diff(u[:9]) >= 0)
 
 
@@ -256,7 +259,8 @@ def test_depth_cap_is_reported(gpu_lib):
     st = calc.stats()
     assert st["n_capped"] > 0
     Lo = Oracle(b).lengths()
-    assert np.max(np.abs(calc.getAllCurveArclengths() - Lo) / Lo) < 1e-6
+    # capped panels miss rtol; the result is still a coarse approximation
+    assert np.max(np.abs(calc.getAllCurveArclengths() - Lo) / Lo) < 1e-3
 
 
 def test_results_are_deterministic(gpu_lib):

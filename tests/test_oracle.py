@@ -68,6 +68,46 @@ def test_mixed_batch_lengths_equal_per_kind_runs():
     np.testing.assert_array_equal(L[5:], Oracle(s).lengths())
 
 
+def test_oracle_rejects_mismatched_counts():
+    b = ds.uniform_bsplines(3, n_ctrl=8, n_samples=4, seed=1)
+    o = Oracle(b)
+    with pytest.raises(ValueError):
+        o.s_at([4], np.zeros(4))  # 1 count for 3 curves
+    with pytest.raises(ValueError):
+        o.reverse([4, 4, 4], np.zeros(11))
+    with pytest.raises(IndexError):
+        o.point(3, 0.5)
+
+
+def _repeated_knot_curve():
+    kv = np.array([0, 0, 0, 0, 0.3, 0.3, 0.3, 0.7, 1, 1, 1, 1.0])
+    pts = np.random.default_rng(0).normal(size=(8, 2)).cumsum(0)
+    return ds._pack([1], [3], [2], [12], kv, [16], pts.ravel(), [5], "rep", 1e-10), kv, pts
+
+
+def test_zero_width_spans_add_nothing():
+    # the length with a triple interior knot equals the sum over the non-degenerate spans,
+    # measured by splitting the curve at the knot into two clamped pieces
+    b, kv, pts = _repeated_knot_curve()
+    L = Oracle(b).lengths()[0]
+    assert np.isfinite(L)
+    # the curve interpolates its control point 3 at t = 0.3 (C0 joint): it is the union of
+    # the cubic pieces on [0, 0.3] and [0.3, 1]
+    left = ds._pack([1], [3], [2], [8], np.array([0, 0, 0, 0, 1, 1, 1, 1.0]), [8], pts[:4].ravel(), [0], "l", 1e-10)
+    kr = np.array([0.3, 0.3, 0.3, 0.3, 0.7, 1, 1, 1, 1.0])
+    right = ds._pack([1], [3], [2], [9], kr, [10], pts[3:].ravel(), [0], "r", 1e-10)
+    assert L == pytest.approx(Oracle(left).lengths()[0] + Oracle(right).lengths()[0], rel=1e-13)
+
+
+@pytest.mark.skipif(not reference_available(), reason="reference tree not present on this host")
+def test_reference_returns_nan_on_repeated_knots():
+    # documents the reference behaviour the oracle deliberately departs from:
+    # its de Boor divides 0 by 0 on a zero-width span
+    b, _, _ = _repeated_knot_curve()
+    Lr, _ = Reference(b).run()
+    assert np.isnan(Lr[0])
+
+
 @pytest.mark.skipif(not reference_available(), reason="reference tree not present on this host")
 def test_port_matches_live_reference_random():
     rng = np.random.default_rng(99)
