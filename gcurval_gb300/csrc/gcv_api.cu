@@ -633,6 +633,13 @@ const char* gcv_status_string(gcv_status s)
 
 const char* gcv_last_error(void) { return g_err.c_str(); }
 
+// Sets the calling thread's gcv_last_error() message (used by the other
+// translation units of the library; not part of the public header).
+__attribute__((visibility("hidden"))) gcv_status gcv_internal_fail(gcv_status s, const char* msg)
+{
+    return fail(s, msg);
+}
+
 int gcv_version(void) { return 100; }
 
 gcv_status gcv_default_options(gcv_options* opt, int precision)

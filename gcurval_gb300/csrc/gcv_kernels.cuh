@@ -117,7 +117,7 @@ __device__ inline void setup_ellipse_seg(const Batch& b, const Table& t, int64_t
     t.seg_f0[s] = PI * fabs(bb);
 }
 
-__global__ void k_setup(Batch b, Table t)
+static __global__ void k_setup(Batch b, Table t)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < b.n_seg;
          s += (int64_t)gridDim.x * blockDim.x) {
@@ -136,7 +136,7 @@ __global__ void k_setup(Batch b, Table t)
 }
 
 // segment -> curve map (thread per curve writes its range)
-__global__ void k_seg_curve(Batch b, int* seg_curve)
+static __global__ void k_seg_curve(Batch b, int* seg_curve)
 {
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < b.n_curve;
          c += (int64_t)gridDim.x * blockDim.x) {
@@ -186,7 +186,7 @@ __device__ __forceinline__ SegVal shfl_up_sv(const SegVal& x, int d)
     return y;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, int64_t n_tiles)
+static __global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, int64_t n_tiles)
 {
     __shared__ int s_tile;
     __shared__ SegVal s_warp[SCAN_THREADS / 32];
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, int64_t
     }
 }
 
-__global__ void k_curve_len(Batch b, Table t)
+static __global__ void k_curve_len(Batch b, Table t)
 {
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < b.n_curve;
          c += (int64_t)gridDim.x * blockDim.x) {

@@ -207,6 +207,34 @@ gcv_status gcv_get_shape(gcv_ctx* ctx, int64_t* n_curve, int64_t* n_segments, in
  * counterpart. */
 gcv_status gcv_measure_fma_peak(int which, double* tflops);
 
+/* ---- allocation-free lengths ---------------------------------------------- */
+
+/* Largest number of knot intervals gcv_bspline_lengths_noalloc accepts. */
+#define GCV_NOALLOC_MAX_INTERVALS 1048576
+
+/* Total length of every curve of a B-spline batch, for callers that cannot
+ * allocate device memory: services that reserve a fixed device-memory budget
+ * at start-up and forbid allocation afterwards, and code running inside
+ * another library's allocator or memory-pool hooks, where a nested cudaMalloc
+ * would recurse or fail.  No counterpart in the reference.
+ *
+ * Same layout as gcv_create_bsplines, but every array is DEVICE memory:
+ * knots_offset[n_curve + 1], knot_vector, ctrl_pts, and the output
+ * lengths[n_curve].  The result equals gcv_create_arclength_table +
+ * gcv_get_all_curve_arclengths (FP64, same rtol / max_depth) to rounding.
+ * The call allocates nothing: its working memory is one static device array
+ * of GCV_NOALLOC_MAX_INTERVALS doubles plus a 256-byte header (about 8 MiB),
+ * held by every GPU that loads the library until the process exits; batches
+ * with more knot intervals return GCV_ERR_INVALID.  The first call on a device
+ * looks up that array's address with the device current; make it before any
+ * stream capture.  All calls share the array, so calls whose GPU work
+ * overlaps race and must be serialised by the caller.  Runs on `stream`
+ * (cudaStream_t, NULL = legacy default stream) and waits for it before
+ * returning. */
+gcv_status gcv_bspline_lengths_noalloc(int n_curve, int degree, int dim, const int* knots_offset,
+                                       const double* knot_vector, const double* ctrl_pts, double rtol,
+                                       int max_depth, double* lengths, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
