@@ -129,17 +129,17 @@ struct gcv_ctx {
     std::vector<double> h_start;  // first parameter value of each curve
 
     // table
-    DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_len, seg_cum, curve_len;
+    DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_q0, seg_len, seg_cum, curve_len;
     DBuf<int64_t> leaf_off;
     DBuf<int> leaf_cnt;
-    DBuf<double> leaf_v, leaf_cum, leaf_f;
+    DBuf<double> leaf_v, leaf_cum, leaf_f, leaf_q;
     int64_t leaf_cap = 0;
     DBuf<int> deep_list;
     DBuf<unsigned long long> ctr;
     DBuf<int> scan_status, scan_flag;
     DBuf<double> scan_hi, scan_lo;
     bool table_ready = false;
-    mixed::MixedState mixed;
+    DBuf<float2> coef_ff;  // float-float copy of coef (GCV_MIXED)
 
     // sampling scratch
     DBuf<int64_t> sample_off;
@@ -182,6 +182,7 @@ Table table_view(gcv_ctx* c)
     t.seg_t0 = c->seg_t0.p;
     t.seg_t1 = c->seg_t1.p;
     t.seg_f0 = c->seg_f0.p;
+    t.seg_q0 = c->seg_q0.p;
     t.seg_len = c->seg_len.p;
     t.seg_cum = c->seg_cum.p;
     t.curve_len = c->curve_len.p;
@@ -190,6 +191,7 @@ Table table_view(gcv_ctx* c)
     t.leaf_v = c->leaf_v.p;
     t.leaf_cum = c->leaf_cum.p;
     t.leaf_f = c->leaf_f.p;
+    t.leaf_q = c->leaf_q.p;
     t.leaf_cap = c->leaf_cap;
     t.deep_list = c->deep_list.p;
     t.deep_cap = (int64_t)c->deep_list.n;
@@ -229,6 +231,7 @@ void destroy_ctx(gcv_ctx* c)
     c->seg_t0.release();
     c->seg_t1.release();
     c->seg_f0.release();
+    c->seg_q0.release();
     c->seg_len.release();
     c->seg_cum.release();
     c->curve_len.release();
@@ -237,6 +240,7 @@ void destroy_ctx(gcv_ctx* c)
     c->leaf_v.release();
     c->leaf_cum.release();
     c->leaf_f.release();
+    c->leaf_q.release();
     c->deep_list.release();
     c->ctr.release();
     c->scan_status.release();
@@ -247,7 +251,7 @@ void destroy_ctx(gcv_ctx* c)
     c->sample_cnt.release();
     c->sample_pos.release();
     c->sample_out.release();
-    mixed::release(c->mixed);
+    c->coef_ff.release();
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -381,6 +385,7 @@ gcv_status ensure_table_buffers(gcv_ctx* c)
     CHECK(c->seg_t0.reserve(ns));
     CHECK(c->seg_t1.reserve(ns));
     CHECK(c->seg_f0.reserve(ns));
+    CHECK(c->seg_q0.reserve(ns));
     CHECK(c->seg_len.reserve(ns));
     CHECK(c->seg_cum.reserve(ns));
     CHECK(c->leaf_off.reserve(ns));
@@ -391,6 +396,7 @@ gcv_status ensure_table_buffers(gcv_ctx* c)
         CHECK(c->leaf_v.reserve((size_t)c->leaf_cap));
         CHECK(c->leaf_cum.reserve((size_t)c->leaf_cap));
         CHECK(c->leaf_f.reserve((size_t)c->leaf_cap));
+        CHECK(c->leaf_q.reserve((size_t)c->leaf_cap));
     }
     if (c->deep_list.n == 0) CHECK(c->deep_list.reserve(ns / 64 + 1024));
     const size_t tiles = (ns + SCAN_TILE - 1) / SCAN_TILE;
@@ -404,7 +410,7 @@ gcv_status ensure_table_buffers(gcv_ctx* c)
 // grows the leaf pool to `cap`, keeping the first `keep` leaves
 gcv_status grow_pool(gcv_ctx* c, int64_t cap, int64_t keep)
 {
-    DBuf<double>* bufs[3] = {&c->leaf_v, &c->leaf_cum, &c->leaf_f};
+    DBuf<double>* bufs[4] = {&c->leaf_v, &c->leaf_cum, &c->leaf_f, &c->leaf_q};
     for (DBuf<double>* b : bufs) {
         DBuf<double> nb;
         CHECK(nb.reserve((size_t)cap));
@@ -426,42 +432,45 @@ gcv_status read_counters(gcv_ctx* c)
     return GCV_OK;
 }
 
-template <int MODE>
-gcv_status launch_length(gcv_ctx* c, const LengthParams& P)
+template <int MODE, int CODE, int PREC>
+gcv_status launch_length_k(gcv_ctx* c, const LengthParams& P)
 {
     int occ = 0;
-    cudaError_t e;
-    switch (c->code) {
-    case CODE_ELLIPSE:
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, CODE_ELLIPSE>, LK_THREADS, 0);
-        break;
-    case bs_code(3, 2):
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, bs_code(3, 2)>, LK_THREADS, 0);
-        break;
-    case bs_code(3, 3):
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, bs_code(3, 3)>, LK_THREADS, 0);
-        break;
-    default: e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, -1>, LK_THREADS, 0); break;
-    }
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, CODE, PREC>, LK_THREADS, 0);
     if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
     occ = std::max(1, std::min(occ, 32));
     // persistent: fill the GPU, but no more lanes than there are intervals
-    int64_t want = (P.n_items + LK_THREADS - 1) / LK_THREADS;
+    const int64_t want = (P.n_items + LK_THREADS - 1) / LK_THREADS;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * occ, want));
-    switch (c->code) {
-    case CODE_ELLIPSE: k_length<MODE, CODE_ELLIPSE><<<grid, LK_THREADS, 0, c->stream>>>(P); break;
-    case bs_code(3, 2): k_length<MODE, bs_code(3, 2)><<<grid, LK_THREADS, 0, c->stream>>>(P); break;
-    case bs_code(3, 3): k_length<MODE, bs_code(3, 3)><<<grid, LK_THREADS, 0, c->stream>>>(P); break;
-    default: k_length<MODE, -1><<<grid, LK_THREADS, 0, c->stream>>>(P); break;
-    }
+    k_length<MODE, CODE, PREC><<<grid, LK_THREADS, 0, c->stream>>>(P);
     CU(cudaGetLastError());
     c->stats.n_launches++;
     return GCV_OK;
 }
 
-gcv_status build_table_fp64(gcv_ctx* c)
+// specialised kernels for the common uniform batches, the runtime dispatch otherwise
+template <int MODE, int PREC>
+gcv_status launch_length_p(gcv_ctx* c, const LengthParams& P)
+{
+    switch (c->code) {
+    case CODE_ELLIPSE: return launch_length_k<MODE, CODE_ELLIPSE, PREC>(c, P);
+    case bs_code(3, 2): return launch_length_k<MODE, bs_code(3, 2), PREC>(c, P);
+    case bs_code(3, 3): return launch_length_k<MODE, bs_code(3, 3), PREC>(c, P);
+    default: return launch_length_k<MODE, -1, PREC>(c, P);
+    }
+}
+
+template <int MODE>
+gcv_status launch_length(gcv_ctx* c, const LengthParams& P)
+{
+    return c->opt.precision == GCV_MIXED ? launch_length_p<MODE, 1>(c, P) : launch_length_p<MODE, 0>(c, P);
+}
+
+gcv_status build_table(gcv_ctx* c)
 {
     CHECK(ensure_table_buffers(c));
+    const bool mixed = c->opt.precision == GCV_MIXED;
+    if (mixed) CHECK(c->coef_ff.reserve((size_t)std::max<int64_t>(c->n_coef, 1)));
     const Batch b = batch_view(c);
     const int setup_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 64));
     CU(cudaEventRecord(c->ev[0], c->stream));
@@ -470,6 +479,12 @@ gcv_status build_table_fp64(gcv_ctx* c)
         k_setup<<<setup_blocks, 256, 0, c->stream>>>(b, table_view(c));
         CU(cudaGetLastError());
         c->stats.n_launches++;
+        if (mixed) {
+            const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_coef + 255) / 256, (int64_t)sm_count() * 64));
+            k_coef_ff<<<blocks, 256, 0, c->stream>>>(c->coef.p, c->coef_ff.p, c->n_coef);
+            CU(cudaGetLastError());
+            c->stats.n_launches++;
+        }
     }
     CU(cudaEventRecord(c->ev[1], c->stream));
     for (int attempt = 0;; ++attempt) {
@@ -480,10 +495,12 @@ gcv_status build_table_fp64(gcv_ctx* c)
         P.b = b;
         P.t = table_view(c);
         P.rtol = c->opt.rtol;
-        P.max_depth = c->opt.max_depth;
+        // float-float panel bounds are exact to depth 44
+        P.max_depth = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
         P.collect = c->opt.collect_stats;
         P.list = nullptr;
         P.n_items = c->n_seg;
+        P.coef_ff = c->coef_ff.p;
         if (c->n_seg > 0) CHECK(launch_length<0>(c, P));
         CHECK(read_counters(c));
         const unsigned long long err = c->h_ctr[C_ERR];
@@ -562,10 +579,7 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, const double* d
     if (total == 0) return GCV_OK;
     CU(cudaEventRecord(c->ev[4], c->stream));
     if (c->opt.collect_stats) CU(cudaMemsetAsync(c->ctr.p + C_NEWTON, 0, sizeof(unsigned long long), c->stream));
-    if (c->opt.precision == GCV_MIXED) {
-        CHECK(mixed::sample(c->mixed, c->stream, batch_view(c), table_view(c), d_sample_off, d_pos, total, is_relative,
-                            what, c->point_dim, d_out, c->opt.collect_stats));
-    } else {
+    {
         SampleParams P;
         P.b = batch_view(c);
         P.t = table_view(c);
@@ -577,13 +591,24 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, const double* d
         P.out = d_out;
         P.n_samples = total;
         P.collect = c->opt.collect_stats;
+        P.rtol = c->opt.rtol;
         const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((total + SAMPLE_THREADS - 1) / SAMPLE_THREADS,
                                                                    (int64_t)sm_count() * 64));
-        switch (c->code) {
-        case CODE_ELLIPSE: k_sample<CODE_ELLIPSE><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
-        case bs_code(3, 2): k_sample<bs_code(3, 2)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
-        case bs_code(3, 3): k_sample<bs_code(3, 3)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
-        default: k_sample<-1><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+        if (c->opt.precision == GCV_MIXED) {
+            const float2* cf = c->coef_ff.p;
+            switch (c->code) {
+            case CODE_ELLIPSE: k_sample_ff<CODE_ELLIPSE><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P, cf); break;
+            case bs_code(3, 2): k_sample_ff<bs_code(3, 2)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P, cf); break;
+            case bs_code(3, 3): k_sample_ff<bs_code(3, 3)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P, cf); break;
+            default: k_sample_ff<-1><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P, cf); break;
+            }
+        } else {
+            switch (c->code) {
+            case CODE_ELLIPSE: k_sample<CODE_ELLIPSE><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+            case bs_code(3, 2): k_sample<bs_code(3, 2)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+            case bs_code(3, 3): k_sample<bs_code(3, 3)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+            default: k_sample<-1><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+            }
         }
         CU(cudaGetLastError());
         c->stats.n_launches++;
@@ -824,14 +849,7 @@ gcv_status gcv_create_arclength_table(gcv_ctx* ctx)
     if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
     ctx->table_ready = false;
     ctx->h_len_valid = false;
-    if (ctx->opt.precision == GCV_MIXED) {
-        CHECK(ensure_table_buffers(ctx));
-        CHECK(mixed::build_table(ctx->mixed, ctx->stream, batch_view(ctx), table_view(ctx), ctx->code, ctx->opt.rtol,
-                                 ctx->opt.max_depth, ctx->opt.collect_stats, ctx->ev, &ctx->stats, ctx->h_ctr,
-                                 ctx->leaf_cap));
-    } else {
-        CHECK(build_table_fp64(ctx));
-    }
+    CHECK(build_table(ctx));
     ctx->table_ready = true;
     return GCV_OK;
 }

@@ -136,6 +136,36 @@ __device__ __forceinline__ double bs_speed(const double* b, double v)
     return sqrt(s);
 }
 
+// f = |g(v)| and q = g(v) . g'(v) (so df/dv = q / f): Horner for the value
+// and its derivative in one pass.
+template <int P, int D>
+__device__ __forceinline__ double bs_speed_slope(const double* b, double v, double& q)
+{
+    double s = 0.0, t = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        double acc = b[(P - 1) * D + d], dacc = 0.0;
+#pragma unroll
+        for (int k = P - 2; k >= 0; --k) {
+            dacc = fma(dacc, v, acc);
+            acc = fma(acc, v, b[k * D + d]);
+        }
+        s = d == 0 ? acc * acc : fma(acc, acc, s);
+        t = d == 0 ? acc * dacc : fma(acc, dacc, t);
+    }
+    q = t;
+    return sqrt(s);
+}
+
+// ellipse: f^2 = pi^2 (B + A sin^2(pi v)), so q = f f' = pi^3 A sin cos
+__device__ __forceinline__ double ellipse_speed_slope(double A, double B, double v, double& q)
+{
+    double s, c;
+    sincospi(v, &s, &c);
+    q = PI * PI * PI * A * s * c;
+    return PI * sqrt(fma(A * s, s, B));
+}
+
 template <int P, int D>
 __device__ __forceinline__ void bs_point(const double* a, double v, double* out)
 {
@@ -175,6 +205,14 @@ struct Eval {
             return ellipse_speed(r[0], r[1], v);
         else
             return bs_speed<P, D>(r, v);
+    }
+    // speed and q = f * df/dv
+    __device__ __forceinline__ static double speed_slope(const double* r, double v, double& q)
+    {
+        if constexpr (CODE == 0)
+            return ellipse_speed_slope(r[0], r[1], v, q);
+        else
+            return bs_speed_slope<P, D>(r, v, q);
     }
     // point at local v (writes D doubles; ellipses apply rotation and centre)
     __device__ __forceinline__ static void point(const double* __restrict__ seg, double v, double* out)
@@ -218,6 +256,17 @@ __device__ __forceinline__ double speed_dyn(int code, const double* r, double v)
         GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
     default: return 0.0;
+    }
+}
+
+__device__ __forceinline__ double speed_slope_dyn(int code, const double* r, double v, double& q)
+{
+    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: return Eval<C>::speed_slope(r, v, q);
+        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+    default: q = 0.0; return 0.0;
     }
 }
 

@@ -1,0 +1,95 @@
+// Float-float ("double-float") arithmetic on the FP32 pipes.
+//
+// A value is an unevaluated sum hi + lo of two floats with |lo| <= ulp(hi)/2,
+// about 48 significant bits.  The building blocks are the published
+// error-free transformations: Knuth's TwoSum, Dekker's Fast2Sum, and the
+// FMA-based exact product (TwoProd).  Every operation below is a handful of
+// FP32 instructions; on GB300 an FP32 instruction costs 1/75 of an FP64 one,
+// so a float-float polynomial evaluation is several times cheaper than the
+// same evaluation in FP64 while keeping ~1e-14 relative accuracy.
+//
+// Nothing here may be compiled with fast-math (it relies on IEEE rounding and
+// on the compiler not reassociating additions; the files are built without
+// --use_fast_math and multiply-adds are written as explicit fmaf).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace gcv {
+
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff ff_from_double(double x)
+{
+    const float h = __double2float_rn(x);
+    return ff{h, __double2float_rn(x - (double)h)};
+}
+
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+
+// Knuth TwoSum: s + e == a + b exactly
+__device__ __forceinline__ ff two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return ff{s, e};
+}
+
+// Dekker Fast2Sum (|a| >= |b|)
+__device__ __forceinline__ ff fast_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    return ff{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+// a + b, "sloppy" variant: error relative to |a| + |b|
+__device__ __forceinline__ ff ff_add(ff a, ff b)
+{
+    const ff s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ ff ff_add_f(ff a, float b)
+{
+    const ff s = two_sum(a.hi, b);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+
+__device__ __forceinline__ ff ff_neg(ff a) { return ff{-a.hi, -a.lo}; }
+
+// a * b with the exact product of the high parts
+__device__ __forceinline__ ff ff_mul(ff a, ff b)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float e = fmaf(a.hi, b.hi, -p);
+    return fast_two_sum(p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e)));
+}
+
+__device__ __forceinline__ ff ff_mul_f(ff a, float b)
+{
+    const float p = __fmul_rn(a.hi, b);
+    const float e = fmaf(a.hi, b, -p);
+    return fast_two_sum(p, fmaf(a.lo, b, e));
+}
+
+// exact scaling by a power of two
+__device__ __forceinline__ ff ff_scale(ff a, float pow2) { return ff{a.hi * pow2, a.lo * pow2}; }
+
+// a * b + c
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) { return ff_add(ff_mul(a, b), c); }
+
+// sqrt: s = a * rsqrt(a) (a few ulp), then one Newton correction
+// s + (a - s^2) / (2 s) with the residual a - s^2 formed exactly by an FMA.
+__device__ __forceinline__ ff ff_sqrt(ff a)
+{
+    if (!(a.hi > 0.0f)) return ff{a.hi == 0.0f ? 0.0f : __fsqrt_rn(a.hi), 0.0f};
+    const float y = rsqrtf(a.hi);
+    const float s = __fmul_rn(a.hi, y);
+    const float r = __fadd_rn(fmaf(-s, s, a.hi), a.lo);
+    return fast_two_sum(s, __fmul_rn(r, 0.5f * y));
+}
+
+}  // namespace gcv

@@ -43,6 +43,7 @@ struct Table {
     double* seg_t0;    // curve parameter at v = -1
     double* seg_t1;    // curve parameter at v = +1
     double* seg_f0;    // f(-1)
+    double* seg_q0;    // (f f')(-1)
     double* seg_len;   // length of each segment
     double* seg_cum;   // cumulative length at the end of each segment (within its curve)
     double* curve_len;
@@ -51,6 +52,7 @@ struct Table {
     double* leaf_v;    // right end (local v) of each leaf panel
     double* leaf_cum;  // cumulative length within the segment at that end
     double* leaf_f;    // f at that end
+    double* leaf_q;    // f * df/dv at that end
     int64_t leaf_cap;
     int* deep_list;
     int64_t deep_cap;
@@ -88,12 +90,15 @@ __device__ void setup_bspline_seg(const Batch& b, const Table& t, int64_t s, int
         bspline_setup<P, D>(kv, cp, span, out);
         t.seg_t0[s] = ka;
         t.seg_t1[s] = kb;
-        t.seg_f0[s] = Eval<bs_code(P, D)>::speed(out + (P + 1) * D, -1.0);
+        double q0;
+        t.seg_f0[s] = Eval<bs_code(P, D)>::speed_slope(out + (P + 1) * D, -1.0, q0);
+        t.seg_q0[s] = q0;
     } else {
         for (int i = 0; i < code_stride(bs_code(P, D)); ++i) out[i] = 0.0;
         t.seg_t0[s] = ka;
         t.seg_t1[s] = ka;
         t.seg_f0[s] = 0.0;
+        t.seg_q0[s] = 0.0;
     }
 }
 
@@ -115,6 +120,7 @@ __device__ inline void setup_ellipse_seg(const Batch& b, const Table& t, int64_t
     t.seg_t0[s] = 0.0;
     t.seg_t1[s] = 2.0 * PI;
     t.seg_f0[s] = PI * fabs(bb);
+    t.seg_q0[s] = 0.0;  // sin(pi v) = 0 at v = -1
 }
 
 static __global__ void k_setup(Batch b, Table t)
@@ -316,6 +322,7 @@ struct SampleParams {
     double* out;
     int64_t n_samples;
     int collect;
+    double rtol;  // the table's tolerance: samples are placed to 1 % of rtol * L
 };
 
 constexpr int SAMPLE_THREADS = 256;
@@ -328,6 +335,61 @@ __device__ __forceinline__ double speed_of(int code, const double* r, double v)
         return Eval<CODE>::speed(r, v);
     else
         return speed_dyn(code, r, v);
+}
+
+template <int CODE>
+__device__ __forceinline__ double speed_slope_of(int code, const double* r, double v, double& q)
+{
+    if constexpr (CODE >= 0)
+        return Eval<CODE>::speed_slope(r, v, q);
+    else
+        return speed_slope_dyn(code, r, v, q);
+}
+
+// Newton on one leaf [va, vb] (cumulative lengths base, cb) for the target rr,
+// from the guess vg: F(v) = S(v) - rr with S(v) = S(va) + GL8(va, v) or
+// S(vb) - GL8(v, vb), whichever side of v is shorter (at most half a leaf,
+// where GL8 is far more accurate than the leaf's own G7 error estimate);
+// bracketed by bisection.  Stops once the residual after the step,
+// about |f'(v)| dn^2 / 2, is below eps_s.
+template <int C>
+__device__ __forceinline__ double leaf_newton(const double* __restrict__ seg, double va, double vb, double base,
+                                              double cb, double rr, double vg, double eps_s,
+                                              unsigned long long& newton)
+{
+    double r[MAX_COEF];
+    Eval<C>::load_speed(seg, r);
+    double blo = va, bhi = vb, v = vg;
+    for (int it = 0; it < NEWTON_MAXIT; ++it) {
+        ++newton;
+        const bool from_left = (v - va) <= (vb - v);
+        const double a0 = from_left ? va : v, a1 = from_left ? v : vb;
+        const double h2 = 0.5 * (a1 - a0);
+        const double m2 = a0 + h2;
+        double I = 0.0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const double xk = h2 * gl8_x(k);
+            I = fma(gl8_w(k), Eval<C>::speed(r, m2 - xk) + Eval<C>::speed(r, m2 + xk), I);
+        }
+        const double F = (from_left ? base + I * h2 : cb - I * h2) - rr;
+        if (F == 0.0) break;
+        if (F < 0.0)
+            blo = v;
+        else
+            bhi = v;
+        double qv;
+        const double fv = Eval<C>::speed_slope(r, v, qv);
+        const double dn = F / fv;
+        if (0.5 * fabs(qv) * dn * dn <= eps_s * fv) {  // converged after this step
+            v = fmin(fmax(v - dn, va), vb);
+            break;
+        }
+        double vn = v - dn;
+        if (!(vn > blo && vn < bhi)) vn = 0.5 * (blo + bhi);  // safeguard (also NaN)
+        v = vn;
+    }
+    return v;
 }
 
 template <int CODE>
@@ -368,63 +430,45 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) k_sample(SampleParams P)
                 const double base = j ? t.leaf_cum[lo + j - 1] : 0.0;
                 const double va = j ? t.leaf_v[lo + j - 1] : -1.0;
                 const double fa = j ? t.leaf_f[lo + j - 1] : t.seg_f0[s];
+                const double qa = j ? t.leaf_q[lo + j - 1] : t.seg_q0[s];
                 const double vb = t.leaf_v[lo + j];
                 const double cb = t.leaf_cum[lo + j];
                 const double fb = t.leaf_f[lo + j];
+                const double qb = t.leaf_q[lo + j];
                 const double dS = cb - base, dv = vb - va;
-                // initial guess: cubic Hermite of v(S) with slopes 1/f at the ends
+                // initial guess: quintic Hermite of the inverse map v(S) on the
+                // leaf, from v' = 1/f and v'' = -f'/f^3 = -q/f^4 at both ends
                 double sig = dS > 0.0 ? (rr - base) / dS : 0.0;
                 sig = fmin(fmax(sig, 0.0), 1.0);
                 double vg = va + sig * dv;
                 const double fm = dS / dv;
                 if (fa > 0.1 * fm && fb > 0.1 * fm) {
-                    const double s2 = sig * sig, s3 = s2 * sig;
-                    const double h10 = s3 - 2.0 * s2 + sig, h11 = s3 - s2;
-                    const double h01 = 3.0 * s2 - 2.0 * s3;
-                    vg = va + h01 * dv + dS * (h10 / fa + h11 / fb);
+                    const double s2 = sig * sig, s3 = s2 * sig, s4 = s3 * sig, s5 = s4 * sig;
+                    const double h5 = 10.0 * s3 - 15.0 * s4 + 6.0 * s5;
+                    const double h1 = sig - 6.0 * s3 + 8.0 * s4 - 3.0 * s5;
+                    const double h4 = -4.0 * s3 + 7.0 * s4 - 3.0 * s5;
+                    const double h2 = 0.5 * (s2 - 3.0 * s3 + 3.0 * s4 - s5);
+                    const double h3 = 0.5 * (s3 - 2.0 * s4 + s5);
+                    const double ia = 1.0 / fa, ib = 1.0 / fb;
+                    const double ka = -qa * (ia * ia) * (ia * ia), kb = -qb * (ib * ib) * (ib * ib);
+                    vg = va + h5 * dv + dS * (h1 * ia + h4 * ib) + dS * dS * (h2 * ka + h3 * kb);
                     vg = fmin(fmax(vg, va), vb);
                 }
                 const double* seg = t.coef + b.coef_off[c] + (s - s0) * code_stride(code);
-                double r[MAX_COEF];
-                if constexpr (CODE >= 0)
-                    Eval<(CODE >= 0 ? CODE : 0)>::load_speed(seg, r);
-                else
-                    load_speed_dyn(code, seg, r);
-                double blo = va, bhi = vb;
-                v = vg;
-                // a step below 1e-7 of the leaf leaves an error of order
-                // (f'/f) * step^2: below 1e-14 of the leaf
-                const double stop = 1e-7 * dv;
-                for (int it = 0; it < NEWTON_MAXIT; ++it) {
-                    ++newton;
-                    // integrate over the shorter side of v: S(v) = S(va) + GL8(va, v)
-                    // or S(vb) - GL8(v, vb); at most half a leaf, where GL8 is far
-                    // more accurate than the leaf's own G7 error estimate
-                    const bool from_left = (v - va) <= (vb - v);
-                    const double a0 = from_left ? va : v, a1 = from_left ? v : vb;
-                    const double h2 = 0.5 * (a1 - a0);
-                    const double m2 = a0 + h2;
-                    double I = 0.0;
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) {
-                        const double xk = h2 * gl8_x(k);
-                        I = fma(gl8_w(k), speed_of<CODE>(code, r, m2 - xk) + speed_of<CODE>(code, r, m2 + xk), I);
+                // After a Newton step dn from v the residual is about |f'(v)| dn^2 / 2;
+                // stop when that is below 1 % of the sample tolerance rtol * L
+                // (tested as |q| dn^2 / 2 <= eps_s f, with q = f f', no division).
+                const double eps_s = 0.01 * P.rtol * L;
+                if constexpr (CODE >= 0) {
+                    v = leaf_newton<(CODE >= 0 ? CODE : 0)>(seg, va, vb, base, cb, rr, vg, eps_s, newton);
+                } else {
+                    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: v = leaf_newton<C>(seg, va, vb, base, cb, rr, vg, eps_s, newton); break;
+                        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+                    default: v = vg; break;
                     }
-                    const double F = (from_left ? base + I * h2 : cb - I * h2) - rr;
-                    if (F == 0.0) break;
-                    if (F < 0.0)
-                        blo = v;
-                    else
-                        bhi = v;
-                    const double fv = speed_of<CODE>(code, r, v);
-                    const double dn = F / fv;
-                    if (fabs(dn) <= stop) {  // converged: the next step would be below 1e-18 of the leaf
-                        v = fmin(fmax(v - dn, va), vb);
-                        break;
-                    }
-                    double vn = v - dn;
-                    if (!(vn > blo && vn < bhi)) vn = 0.5 * (blo + bhi);  // safeguard (also NaN)
-                    v = vn;
                 }
             }
         }

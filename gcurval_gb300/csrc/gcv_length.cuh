@@ -24,6 +24,7 @@
 #pragma once
 
 #include "gcv_kernels.cuh"
+#include "gcv_mixed.cuh"
 
 namespace gcv {
 
@@ -40,12 +41,13 @@ struct LengthParams {
     int collect;
     const int* list;  // segments to process (deep passes); NULL: all segments
     int64_t n_items;
+    const float2* coef_ff;  // float-float copy of the coefficients (PREC 1)
 };
 
 // K15, G7 and the right-end speed of panel [vlo, vlo + 2 hw].
 template <int CODE>
 __device__ __forceinline__ void panel_k15(const double* r, double vlo, double hw, double& K, double& G,
-                                          double& fend)
+                                          double& fend, double& qend)
 {
     const double mid = vlo + hw;
     const double fc = Eval<CODE>::speed(r, mid);
@@ -58,20 +60,20 @@ __device__ __forceinline__ void panel_k15(const double* r, double vlo, double hw
         k = fma(gk_wk(i), s, k);
         if (i & 1) g = fma(gk_wg(i), s, g);
     }
-    fend = Eval<CODE>::speed(r, vlo + 2.0 * hw);
+    fend = Eval<CODE>::speed_slope(r, vlo + 2.0 * hw, qend);
     K = k * hw;
     G = g * hw;
 }
 
 __device__ __forceinline__ void panel_dyn(int code, const double* r, double vlo, double hw, double& K, double& G,
-                                          double& fend)
+                                          double& fend, double& qend)
 {
     switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: panel_k15<C>(r, vlo, hw, K, G, fend); break;
+    case C: panel_k15<C>(r, vlo, hw, K, G, fend, qend); break;
         GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
-    default: K = G = fend = 0.0; break;
+    default: K = G = fend = qend = 0.0; break;
     }
 }
 
@@ -85,12 +87,15 @@ __device__ __forceinline__ int warp_incl_scan(int x, int lane)
     return x;
 }
 
-template <int MODE, int CODE>
+// PREC 0: FP64 panels; PREC 1: float-float panels (GCV_MIXED), whose K15 /
+// G7 / end values enter the same FP64 bookkeeping (error test, leaf table).
+template <int MODE, int CODE, int PREC = 0>
 __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
 {
     __shared__ double lf_v[MODE == 0 ? LCAP : 1][LK_THREADS];
     __shared__ double lf_c[MODE == 0 ? LCAP : 1][LK_THREADS];
     __shared__ double lf_f[MODE == 0 ? LCAP : 1][LK_THREADS];
+    __shared__ double lf_q[MODE == 0 ? LCAP : 1][LK_THREADS];
 
     const Batch& b = P.b;
     const Table& t = P.t;
@@ -98,12 +103,15 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
     const int tid = threadIdx.x;
     const unsigned FULL = 0xffffffffu;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const double eps50 = 50.0 * 2.220446049250313e-16;
+    // round-off floor of the error test: 50 units of the working precision
+    // (FP64: 2^-52; float-float: ~2^-46)
+    const double eps50 = PREC == 1 ? 50.0 * 1.4210854715202004e-14 : 50.0 * 2.220446049250313e-16;
 
     bool active = false, exhausted = false;
     int64_t s = 0, pool = 0;
     int code = CODE >= 0 ? CODE : 0;
-    double r[MAX_COEF];
+    double r[PREC == 0 ? MAX_COEF : 1];
+    ff rf[PREC == 1 ? MAX_COEF : 1];
     unsigned long long k = 0;
     int depth = 0, nleaf = 0;
     double cum = 0.0, tol_unit = 0.0;
@@ -128,11 +136,18 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                     s = P.list ? (int64_t)P.list[item] : item;
                     const int64_t c = b.seg_curve[s];
                     if (CODE < 0) code = curve_code(b, c);
-                    const double* seg = t.coef + b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
-                    if constexpr (CODE >= 0)
-                        Eval<(CODE >= 0 ? CODE : 0)>::load_speed(seg, r);
-                    else
-                        load_speed_dyn(code, seg, r);
+                    const int64_t ci = b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
+                    if constexpr (PREC == 1) {
+                        if constexpr (CODE >= 0)
+                            EvalFF<(CODE >= 0 ? CODE : 0)>::load(P.coef_ff + ci, rf);
+                        else
+                            load_ff_dyn(code, P.coef_ff + ci, rf);
+                    } else {
+                        if constexpr (CODE >= 0)
+                            Eval<(CODE >= 0 ? CODE : 0)>::load_speed(t.coef + ci, r);
+                        else
+                            load_speed_dyn(code, t.coef + ci, r);
+                    }
                     k = 0;
                     depth = 0;
                     nleaf = 0;
@@ -150,10 +165,12 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                             lf_v[0][tid] = 1.0;
                             lf_c[0][tid] = 0.0;
                             lf_f[0][tid] = 0.0;
+                            lf_q[0][tid] = 0.0;
                         } else if (MODE == 2 && pool >= 0) {
                             t.leaf_v[pool] = 1.0;
                             t.leaf_cum[pool] = 0.0;
                             t.leaf_f[pool] = 0.0;
+                            t.leaf_q[pool] = 0.0;
                         }
                         nleaf = 1;
                         fin = true;
@@ -167,11 +184,24 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
         if (active) {
             const double hw = pow2_neg(depth);
             const double vlo = fma(__ull2double_rn(k), 2.0 * hw, -1.0);
-            double K, G, fend;
-            if constexpr (CODE >= 0)
-                panel_k15<(CODE >= 0 ? CODE : 0)>(r, vlo, hw, K, G, fend);
-            else
-                panel_dyn(code, r, vlo, hw, K, G, fend);
+            double K, G, fend, qend;
+            if constexpr (PREC == 1) {
+                ff Kf, Gf, ff_end;
+                float q32;
+                if constexpr (CODE >= 0)
+                    panel_k15_ff<(CODE >= 0 ? CODE : 0)>(rf, k, depth, Kf, Gf, ff_end, q32);
+                else
+                    panel_ff_dyn(code, rf, k, depth, Kf, Gf, ff_end, q32);
+                K = ff_to_double(Kf);
+                G = ff_to_double(Gf);
+                fend = ff_to_double(ff_end);
+                qend = (double)q32;
+            } else {
+                if constexpr (CODE >= 0)
+                    panel_k15<(CODE >= 0 ? CODE : 0)>(r, vlo, hw, K, G, fend, qend);
+                else
+                    panel_dyn(code, r, vlo, hw, K, G, fend, qend);
+            }
             if (depth == 0) tol_unit = P.rtol * fabs(K);
             ++panels;
             const double err = fabs(K - G);
@@ -188,6 +218,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                         lf_v[nleaf][tid] = vr;
                         lf_c[nleaf][tid] = cum;
                         lf_f[nleaf][tid] = fend;
+                        lf_q[nleaf][tid] = qend;
                     } else {
                         ovf = true;
                     }
@@ -195,6 +226,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                     t.leaf_v[pool + nleaf] = vr;
                     t.leaf_cum[pool + nleaf] = cum;
                     t.leaf_f[pool + nleaf] = fend;
+                    t.leaf_q[pool + nleaf] = qend;
                 }
                 ++nleaf;
                 ++k;
@@ -230,6 +262,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                             t.leaf_v[off + i] = lf_v[i][tid];
                             t.leaf_cum[off + i] = lf_c[i][tid];
                             t.leaf_f[off + i] = lf_f[i][tid];
+                            t.leaf_q[off + i] = lf_q[i][tid];
                         }
                     } else {
                         raise_err(t, ERR_POOL);

@@ -1,30 +1,414 @@
-// Mixed-precision path (FP32 integrand and panels; FP64 prefix sum, error
-// test near tolerance and final Newton step).
+// Mixed-precision path (GCV_MIXED): the integrand and the panel sums run on
+// the FP32 pipes in float-float arithmetic (gcv_ff.cuh, ~48-bit significand);
+// FP64 is kept for the three steps whose stability needs it:
+//   * the compensated prefix sum of interval lengths (k_scan, shared with the
+//     FP64 path),
+//   * the panel error test when the FP32 test lands near the tolerance,
+//   * the final Newton update of every sample's parameter.
+// Plain FP32 integrands (rounding ~3e-8 per evaluation, plus the systematic
+// rounding of each interval's polynomial coefficients) cannot hold a 1e-8
+// relative length on curves of one or a few knot intervals; float-float can,
+// at a fraction of the FP64 cost on GB300 (FP32:FP64 throughput ~75:1).
+//
+// Ellipse integrands (sin(pi v)) are evaluated with an own float-float
+// sin(pi x) (Taylor series after reduction to |x| <= 1/4).
 #pragma once
 
-#include "gcurval_gb300.h"
+#include "gcv_ff.cuh"
 #include "gcv_kernels.cuh"
 
 namespace gcv {
-namespace mixed {
 
-struct MixedState {
-    int unused = 0;
+// float-float constants from double literals (split at compile time)
+struct ffc {
+    float hi, lo;
+};
+__host__ __device__ constexpr ffc split_const(double x)
+{
+    return ffc{(float)x, (float)(x - (double)(float)x)};
+}
+__device__ __forceinline__ ff to_ff(ffc c) { return ff{c.hi, c.lo}; }
+
+// ------------------------------------------------------- sin(pi x), |x| <= 1
+// Reduce x to r in [-1/4, 1/4] with sin(pi x) = +-sin(pi r) or +-cos(pi r),
+// then Taylor series of sin(t), cos(t) in t = pi r (|t| <= pi/4: the 17th /
+// 16th order terms are below 2e-14, far under float-float rounding).
+__device__ __forceinline__ ff ff_sin_taylor(ff t)
+{
+    const ff t2 = ff_mul(t, t);
+    // t * (1 - t^2/3! + t^4/5! - ... + t^16/17!)
+    ff p = to_ff(split_const(1.0 / 355687428096000.0));  // 1/17!
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 1307674368000.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 6227020800.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 39916800.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 362880.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 5040.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 120.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 6.0))));
+    p = ff_fma(p, t2, ff{1.0f, 0.0f});
+    return ff_mul(p, t);
+}
+__device__ __forceinline__ ff ff_cos_taylor(ff t)
+{
+    const ff t2 = ff_mul(t, t);
+    ff p = to_ff(split_const(1.0 / 20922789888000.0));  // 1/16!
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 87178291200.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 479001600.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 3628800.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 40320.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 720.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 24.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(0.5))));
+    return ff_fma(p, t2, ff{1.0f, 0.0f});
+}
+
+// sin(pi x)^2 for x in [-1, 1]
+__device__ __forceinline__ ff ff_sinpi_sq(ff x)
+{
+    // sin^2(pi x) has period 1 and is even: fold to y in [0, 1/2]
+    float ax = fabsf(x.hi);
+    ff y = x.hi < 0.0f ? ff_neg(x) : x;
+    if (ax > 0.5f) y = ff_add_f(ff_neg(y), 1.0f);  // 1 - |x|
+    (void)ax;
+    // y in [0, 1/2]: sin(pi y) = cos(pi (1/2 - y)); use sin for y <= 1/4
+    const ff pi = to_ff(split_const(3.141592653589793238462643383279502884));
+    ff s;
+    if (y.hi <= 0.25f) {
+        s = ff_sin_taylor(ff_mul(pi, y));
+    } else {
+        s = ff_cos_taylor(ff_mul(pi, ff_add_f(ff_neg(y), 0.5f)));
+    }
+    return ff_mul(s, s);
+}
+
+// ------------------------------------------------------------- evaluators
+template <int CODE>
+struct EvalFF {
+    static constexpr int P = code_degree(CODE);
+    static constexpr int D = code_dim(CODE);
+    // derivative polynomial (B-spline) or A, B (ellipse) as float-float
+    __device__ __forceinline__ static void load(const float2* __restrict__ seg, ff* r)
+    {
+        if constexpr (CODE == 0) {
+            r[0] = ff{seg[0].x, seg[0].y};
+            r[1] = ff{seg[1].x, seg[1].y};
+        } else {
+#pragma unroll
+            for (int i = 0; i < P * D; ++i) {
+                const float2 c = seg[(P + 1) * D + i];
+                r[i] = ff{c.x, c.y};
+            }
+        }
+    }
+    __device__ __forceinline__ static ff speed(const ff* r, ff v)
+    {
+        if constexpr (CODE == 0) {
+            // pi * sqrt(B + A sin^2(pi v))
+            const ff s2 = ff_sinpi_sq(v);
+            return ff_mul(to_ff(split_const(PI)), ff_sqrt(ff_fma(r[0], s2, r[1])));
+        } else {
+            ff s{0.0f, 0.0f};
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                ff acc = r[(P - 1) * D + d];
+#pragma unroll
+                for (int k = P - 2; k >= 0; --k) acc = ff_fma(acc, v, r[k * D + d]);
+                s = d == 0 ? ff_mul(acc, acc) : ff_fma(acc, acc, s);
+            }
+            return ff_sqrt(s);
+        }
+    }
+    // speed and q = f * df/dv (q only to FP32 accuracy: it shapes the initial guess
+    // and the stopping test, never the result)
+    __device__ __forceinline__ static ff speed_slope(const ff* r, ff v, float& q)
+    {
+        if constexpr (CODE == 0) {
+            const float vh = v.hi;
+            float sn, cs;
+            sincospif(vh, &sn, &cs);
+            q = (float)(PI * PI * PI) * r[0].hi * sn * cs;
+            return speed(r, v);
+        } else {
+            ff s{0.0f, 0.0f};
+            float t = 0.0f;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                ff acc = r[(P - 1) * D + d];
+                float dacc = 0.0f;
+#pragma unroll
+                for (int k = P - 2; k >= 0; --k) {
+                    dacc = fmaf(dacc, v.hi, acc.hi);
+                    acc = ff_fma(acc, v, r[k * D + d]);
+                }
+                s = d == 0 ? ff_mul(acc, acc) : ff_fma(acc, acc, s);
+                t = fmaf(acc.hi, dacc, t);
+            }
+            q = t;
+            return ff_sqrt(s);
+        }
+    }
 };
 
-inline void release(MixedState&) {}
-
-inline gcv_status build_table(MixedState&, cudaStream_t, const Batch&, const Table&, int, double, int, int, cudaEvent_t*,
-                              gcv_stats*, unsigned long long*, int64_t)
+// float-float panel: K15, G7, right-end speed and slope of [vlo, vlo + 2 hw]
+// with vlo = -1 + k 2^(1-depth) built exactly from the integer k.
+template <int CODE>
+__device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, int depth, ff& K, ff& G, ff& fend,
+                                             float& qend)
 {
-    return GCV_ERR_INVALID;
+    const float hw = __int_as_float((127 - depth) << 23);  // 2^-depth, exact
+    const float kh = (float)(unsigned)(k >> 24), kl = (float)(unsigned)(k & 0xFFFFFFull);
+    const float sh = __int_as_float((127 + 25 - depth) << 23), sl = 2.0f * hw;  // 2^(25-depth), 2^(1-depth)
+    const ff vlo = ff_add_f(two_sum(-1.0f, kh * sh), kl * sl);
+    const ff mid = ff_add_f(vlo, hw);
+    const ff fc = EvalFF<CODE>::speed(r, mid);
+    ff kk = ff_mul(to_ff(split_const(gk_wk(7))), fc);
+    ff gg = ff_mul(to_ff(split_const(gk_wg(7))), fc);
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        const ff dx = ff_scale(to_ff(split_const(gk_x(i))), hw);
+        const ff s = ff_add(EvalFF<CODE>::speed(r, ff_add(mid, ff_neg(dx))), EvalFF<CODE>::speed(r, ff_add(mid, dx)));
+        kk = ff_fma(to_ff(split_const(gk_wk(i))), s, kk);
+        if (i & 1) gg = ff_fma(to_ff(split_const(gk_wg(i))), s, gg);
+    }
+    fend = EvalFF<CODE>::speed_slope(r, ff_add_f(vlo, 2.0f * hw), qend);
+    K = ff_scale(kk, hw);
+    G = ff_scale(gg, hw);
 }
 
-inline gcv_status sample(MixedState&, cudaStream_t, const Batch&, const Table&, const int64_t*, const double*, int64_t,
-                         int, int, int, double*, int)
+__device__ __forceinline__ void load_ff_dyn(int code, const float2* __restrict__ seg, ff* r)
 {
-    return GCV_ERR_INVALID;
+    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: EvalFF<C>::load(seg, r); break;
+        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+    default: break;
+    }
 }
 
-}  // namespace mixed
+__device__ __forceinline__ void panel_ff_dyn(int code, const ff* r, unsigned long long k, int depth, ff& K, ff& G,
+                                             ff& fend, float& qend)
+{
+    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: panel_k15_ff<C>(r, k, depth, K, G, fend, qend); break;
+        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+    default: K = G = fend = ff{0.0f, 0.0f}; qend = 0.0f; break;
+    }
+}
+
+template <int CODE>
+__device__ __forceinline__ ff speed_ff_of(int code, const ff* r, ff v)
+{
+    if constexpr (CODE >= 0) {
+        return EvalFF<CODE>::speed(r, v);
+    } else {
+        switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: return EvalFF<C>::speed(r, v);
+            GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+        default: return ff{0.0f, 0.0f};
+        }
+    }
+}
+
+template <int CODE>
+__device__ __forceinline__ ff speed_slope_ff_of(int code, const ff* r, ff v, float& q)
+{
+    if constexpr (CODE >= 0) {
+        return EvalFF<CODE>::speed_slope(r, v, q);
+    } else {
+        switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: return EvalFF<C>::speed_slope(r, v, q);
+            GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+        default: q = 0.0f; return ff{0.0f, 0.0f};
+        }
+    }
+}
+
+// float-float copy of every segment's evaluation data (same indexing as coef)
+static __global__ void k_coef_ff(const double* __restrict__ coef, float2* __restrict__ out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = coef[i];
+        const float h = __double2float_rn(x);
+        out[i] = make_float2(h, __double2float_rn(x - (double)h));
+    }
+}
+
+// ------------------------------------------------------------- sampling
+// Newton on one leaf in float-float, in the local offset w = v - va in
+// [0, dv]: F(w) = S(va + w) - S(va) - rl with the partial integral taken by
+// 8-point Gauss over the shorter side of the leaf, bracketed by bisection.
+// Returns the final offset, whose last update is done in FP64.
+template <int C>
+__device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg, ff vaf, float dv, ff rl, ff dS,
+                                                 float dvg, float eps_s, unsigned long long& newton)
+{
+    ff r[MAX_COEF];
+    EvalFF<C>::load(seg, r);
+    float blo = 0.0f, bhi = dv;
+    ff w{dvg, 0.0f};
+    double wfinal = dvg;
+    for (int it = 0; it < NEWTON_MAXIT; ++it) {
+        ++newton;
+        const bool from_left = w.hi <= 0.5f * dv;
+        // [a0, a1] in local offsets: [0, w] or [w, dv]
+        const ff a0 = from_left ? ff{0.0f, 0.0f} : w;
+        const ff a1 = from_left ? w : ff{dv, 0.0f};
+        const ff h2 = ff_scale(ff_add(a1, ff_neg(a0)), 0.5f);
+        const ff m2 = ff_add(ff_add(vaf, a0), h2);
+        ff I{0.0f, 0.0f};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const ff xk = ff_mul(h2, to_ff(split_const(gl8_x(k))));
+            const ff sum = ff_add(EvalFF<C>::speed(r, ff_add(m2, ff_neg(xk))), EvalFF<C>::speed(r, ff_add(m2, xk)));
+            I = ff_fma(to_ff(split_const(gl8_w(k))), sum, I);
+        }
+        I = ff_mul(I, h2);
+        // F = S(v) - target inside the leaf
+        const ff F = from_left ? ff_add(I, ff_neg(rl)) : ff_add(ff_add(dS, ff_neg(I)), ff_neg(rl));
+        const float Fh = F.hi + F.lo;
+        if (Fh == 0.0f) {
+            wfinal = (double)w.hi + (double)w.lo;
+            break;
+        }
+        if (Fh < 0.0f)
+            blo = w.hi;
+        else
+            bhi = w.hi;
+        float qv;
+        const ff fv = EvalFF<C>::speed_slope(r, ff_add(vaf, w), qv);
+        const float dn = Fh / fv.hi;
+        if (0.5f * fabsf(qv) * dn * dn <= eps_s * fv.hi) {
+            // converged: the final update in FP64
+            wfinal = ((double)w.hi + (double)w.lo) - (double)dn;
+            break;
+        }
+        const float wn = w.hi - dn;
+        if (!(wn > blo && wn < bhi))
+            w = ff{0.5f * (blo + bhi), 0.0f};  // safeguard (also NaN)
+        else
+            w = ff_add_f(w, -dn);
+        wfinal = (double)w.hi + (double)w.lo;
+    }
+    return wfinal;
+}
+
+// Mixed-precision sampling: table lookups and the target in FP64, the
+// quintic-Hermite guess in FP32, Newton on the leaf in float-float
+// (G8 partial integral on the shorter side, local to the leaf), and the
+// final update of v in FP64.
+template <int CODE>
+__global__ void __launch_bounds__(SAMPLE_THREADS) k_sample_ff(SampleParams P, const float2* __restrict__ coef_ff)
+{
+    const Batch& b = P.b;
+    const Table& t = P.t;
+    unsigned long long newton = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n_samples;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int c = upper_bound_i64(P.sample_off, int(b.n_curve) + 1, i);
+        const int code = CODE >= 0 ? CODE : curve_code(b, c);
+        const int64_t s0 = b.seg_off[c], s1 = b.seg_off[c + 1];
+        int64_t s;
+        double v;
+        if (s1 == s0) {
+            s = -1;
+            v = -1.0;
+        } else {
+            const double L = t.curve_len[c];
+            const double pos = P.pos[i];
+            const double target = P.is_relative ? pos * L : pos;
+            if (!(target > 0.0)) {
+                s = s0;
+                v = -1.0;
+            } else if (target >= L) {
+                s = s1 - 1;
+                v = 1.0;
+            } else {
+                s = lower_bound_key(t.seg_cum, s0, s1, dkey(target));
+                if (s == s1) s = s1 - 1;
+                const double prev = s > s0 ? t.seg_cum[s - 1] : 0.0;
+                const double rr = target - prev;
+                const int64_t lo = t.leaf_off[s];
+                const int cnt = t.leaf_cnt[s];
+                int64_t j = lower_bound_key(t.leaf_cum, lo, lo + cnt, dkey(rr)) - lo;
+                if (j >= cnt) j = cnt - 1;
+                const double base = j ? t.leaf_cum[lo + j - 1] : 0.0;
+                const double va = j ? t.leaf_v[lo + j - 1] : -1.0;
+                const float fa = (float)(j ? t.leaf_f[lo + j - 1] : t.seg_f0[s]);
+                const float qa = (float)(j ? t.leaf_q[lo + j - 1] : t.seg_q0[s]);
+                const double vb = t.leaf_v[lo + j];
+                const double cb = t.leaf_cum[lo + j];
+                const float fb = (float)t.leaf_f[lo + j];
+                const float qb = (float)t.leaf_q[lo + j];
+                const ff rl = ff_from_double(rr - base);   // target inside the leaf
+                const ff dS = ff_from_double(cb - base);   // leaf length
+                const float dv = (float)(vb - va);          // leaf width (exact dyadic)
+                const ff vaf = ff_from_double(va);
+                // quintic Hermite guess of v(S) on the leaf (FP32)
+                float sig = dS.hi > 0.0f ? rl.hi / dS.hi : 0.0f;
+                sig = fminf(fmaxf(sig, 0.0f), 1.0f);
+                float dvg = sig * dv;
+                const float fm = dS.hi / dv;
+                if (fa > 0.1f * fm && fb > 0.1f * fm) {
+                    const float s2 = sig * sig, s3 = s2 * sig, s4 = s3 * sig, s5 = s4 * sig;
+                    const float h5 = 10.0f * s3 - 15.0f * s4 + 6.0f * s5;
+                    const float h1 = sig - 6.0f * s3 + 8.0f * s4 - 3.0f * s5;
+                    const float h4 = -4.0f * s3 + 7.0f * s4 - 3.0f * s5;
+                    const float h2 = 0.5f * (s2 - 3.0f * s3 + 3.0f * s4 - s5);
+                    const float h3 = 0.5f * (s3 - 2.0f * s4 + s5);
+                    const float ia = 1.0f / fa, ib = 1.0f / fb;
+                    const float ka = -qa * (ia * ia) * (ia * ia), kb = -qb * (ib * ib) * (ib * ib);
+                    dvg = h5 * dv + dS.hi * (h1 * ia + h4 * ib) + dS.hi * dS.hi * (h2 * ka + h3 * kb);
+                    dvg = fminf(fmaxf(dvg, 0.0f), dv);
+                }
+                const float2* seg = coef_ff + b.coef_off[c] + (s - s0) * code_stride(code);
+                const float eps_s = (float)(0.01 * P.rtol * L);
+                double wfinal;
+                if constexpr (CODE >= 0) {
+                    wfinal = ff_leaf_newton<(CODE >= 0 ? CODE : 0)>(seg, vaf, dv, rl, dS, dvg, eps_s, newton);
+                } else {
+                    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: wfinal = ff_leaf_newton<C>(seg, vaf, dv, rl, dS, dvg, eps_s, newton); break;
+                        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+                    default: wfinal = dvg; break;
+                    }
+                }
+                v = fmin(fmax(va + wfinal, va), vb);
+            }
+        }
+        if (P.what == 2) {
+            double u;
+            if (s < 0) {
+                u = b.kind[c] == 0 ? 0.0 : b.knots[b.knot_off[c] + b.degree[c]];
+            } else {
+                const double t0 = t.seg_t0[s], t1 = t.seg_t1[s], hw = 0.5 * (t1 - t0);
+                u = v <= 0.0 ? fma(v + 1.0, hw, t0) : fma(v - 1.0, hw, t1);
+            }
+            P.out[i] = u;
+        } else {
+            double p3[3] = {0.0, 0.0, 0.0};
+            if (s >= 0) {
+                const double* seg = t.coef + b.coef_off[c] + (s - s0) * code_stride(code);
+                if constexpr (CODE >= 0)
+                    Eval<(CODE >= 0 ? CODE : 0)>::point(seg, v, p3);
+                else
+                    point_dyn(code, seg, v, p3);
+            }
+            for (int k = 0; k < P.pdim; ++k) P.out[i * P.pdim + k] = p3[k];
+        }
+    }
+    if (P.collect) {
+        for (int o = 16; o > 0; o >>= 1) newton += __shfl_xor_sync(0xffffffffu, newton, o);
+        if ((threadIdx.x & 31) == 0 && newton) atomicAdd(t.ctr + C_NEWTON, newton);
+    }
+}
+
 }  // namespace gcv

@@ -87,8 +87,8 @@ __device__ double interval_length(const double* r, double rtol, int max_depth, u
     for (;;) {
         const double hw = pow2_neg(depth);
         const double vlo = fma(__ull2double_rn(k), 2.0 * hw, -1.0);
-        double K, G, fend;
-        panel_k15<CODE>(r, vlo, hw, K, G, fend);
+        double K, G, fend, qend;
+        panel_k15<CODE>(r, vlo, hw, K, G, fend, qend);
         if (depth == 0) tol_unit = rtol * fabs(K);
         ++panels;
         const double err = fabs(K - G);
