@@ -352,7 +352,14 @@ __device__ __forceinline__ double speed_slope_of(int code, const double* r, doub
 // where GL8 is far more accurate than the leaf's own G7 error estimate);
 // bracketed by bisection.  Stops once the residual after the step,
 // about |f'(v)| dn^2 / 2, is below eps_s.
-template <int C>
+// 8-point Gauss nodes (-x0..-x3, x0..x3) and weights w0..w3 for rolled loops
+static __constant__ double c_gl8[12] = {-gl8_x(0), -gl8_x(1), -gl8_x(2), -gl8_x(3), gl8_x(0), gl8_x(1),
+                                        gl8_x(2),  gl8_x(3),  gl8_w(0),  gl8_w(1),  gl8_w(2), gl8_w(3)};
+
+// UNROLL: fixed-code kernels unroll the Gauss loop; the runtime-dispatch
+// kernel keeps it rolled so that eleven specialised bodies fit the
+// instruction cache.
+template <int C, bool UNROLL = true>
 __device__ __forceinline__ double leaf_newton(const double* __restrict__ seg, double va, double vb, double base,
                                               double cb, double rr, double vg, double eps_s,
                                               unsigned long long& newton)
@@ -367,10 +374,15 @@ __device__ __forceinline__ double leaf_newton(const double* __restrict__ seg, do
         const double h2 = 0.5 * (a1 - a0);
         const double m2 = a0 + h2;
         double I = 0.0;
+        if constexpr (UNROLL) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const double xk = h2 * gl8_x(k);
-            I = fma(gl8_w(k), Eval<C>::speed(r, m2 - xk) + Eval<C>::speed(r, m2 + xk), I);
+            for (int k = 0; k < 4; ++k) {
+                const double xk = h2 * gl8_x(k);
+                I = fma(gl8_w(k), Eval<C>::speed(r, m2 - xk) + Eval<C>::speed(r, m2 + xk), I);
+            }
+        } else {
+#pragma unroll 1
+            for (int k = 0; k < 8; ++k) I = fma(c_gl8[8 + (k & 3)], Eval<C>::speed(r, fma(h2, c_gl8[k], m2)), I);
         }
         const double F = (from_left ? base + I * h2 : cb - I * h2) - rr;
         if (F == 0.0) break;
@@ -464,7 +476,7 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) k_sample(SampleParams P)
                 } else {
                     switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: v = leaf_newton<C>(seg, va, vb, base, cb, rr, vg, eps_s, newton); break;
+    case C: v = leaf_newton<C, false>(seg, va, vb, base, cb, rr, vg, eps_s, newton); break;
                         GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
                     default: v = vg; break;

@@ -245,7 +245,18 @@ static __global__ void k_coef_ff(const double* __restrict__ coef, float2* __rest
 // [0, dv]: F(w) = S(va + w) - S(va) - rl with the partial integral taken by
 // 8-point Gauss over the shorter side of the leaf, bracketed by bisection.
 // Returns the final offset, whose last update is done in FP64.
-template <int C>
+// 8-point Gauss nodes (-x0..-x3, x0..x3) then weights w0..w3, float-float
+#define GCV_FFC(x) {split_const(x).hi, split_const(x).lo}
+static __constant__ float2 c_gl8_ff[12] = {
+    GCV_FFC(-gl8_x(0)), GCV_FFC(-gl8_x(1)), GCV_FFC(-gl8_x(2)), GCV_FFC(-gl8_x(3)),
+    GCV_FFC(gl8_x(0)),  GCV_FFC(gl8_x(1)),  GCV_FFC(gl8_x(2)),  GCV_FFC(gl8_x(3)),
+    GCV_FFC(gl8_w(0)),  GCV_FFC(gl8_w(1)),  GCV_FFC(gl8_w(2)),  GCV_FFC(gl8_w(3))};
+#undef GCV_FFC
+
+// UNROLL: fixed-code kernels unroll the Gauss loop; the runtime-dispatch
+// kernel keeps it rolled so that eleven specialised bodies fit the
+// instruction cache.
+template <int C, bool UNROLL>
 __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg, ff vaf, float dv, ff rl, ff dS,
                                                  float dvg, float eps_s, unsigned long long& newton)
 {
@@ -263,11 +274,18 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
         const ff h2 = ff_scale(ff_add(a1, ff_neg(a0)), 0.5f);
         const ff m2 = ff_add(ff_add(vaf, a0), h2);
         ff I{0.0f, 0.0f};
+        if constexpr (UNROLL) {
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const ff xk = ff_mul(h2, to_ff(split_const(gl8_x(k))));
-            const ff sum = ff_add(EvalFF<C>::speed(r, ff_add(m2, ff_neg(xk))), EvalFF<C>::speed(r, ff_add(m2, xk)));
-            I = ff_fma(to_ff(split_const(gl8_w(k))), sum, I);
+            for (int k = 0; k < 8; ++k) {
+                const ff xk = ff_mul(h2, to_ff(split_const(k < 4 ? -gl8_x(k) : gl8_x(k - 4))));
+                I = ff_fma(to_ff(split_const(gl8_w(k & 3))), EvalFF<C>::speed(r, ff_add(m2, xk)), I);
+            }
+        } else {
+#pragma unroll 1
+            for (int k = 0; k < 8; ++k) {
+                const ff xk = ff_mul(h2, ff{c_gl8_ff[k].x, c_gl8_ff[k].y});
+                I = ff_fma(ff{c_gl8_ff[8 + (k & 3)].x, c_gl8_ff[8 + (k & 3)].y}, EvalFF<C>::speed(r, ff_add(m2, xk)), I);
+            }
         }
         I = ff_mul(I, h2);
         // F = S(v) - target inside the leaf
@@ -371,11 +389,11 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) k_sample_ff(SampleParams P, co
                 const float eps_s = (float)(0.01 * P.rtol * L);
                 double wfinal;
                 if constexpr (CODE >= 0) {
-                    wfinal = ff_leaf_newton<(CODE >= 0 ? CODE : 0)>(seg, vaf, dv, rl, dS, dvg, eps_s, newton);
+                    wfinal = ff_leaf_newton<(CODE >= 0 ? CODE : 0), true>(seg, vaf, dv, rl, dS, dvg, eps_s, newton);
                 } else {
                     switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: wfinal = ff_leaf_newton<C>(seg, vaf, dv, rl, dS, dvg, eps_s, newton); break;
+    case C: wfinal = ff_leaf_newton<C, false>(seg, vaf, dv, rl, dS, dvg, eps_s, newton); break;
                         GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
                     default: wfinal = dvg; break;
