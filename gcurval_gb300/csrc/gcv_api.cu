@@ -179,6 +179,7 @@ Table table_view(gcv_ctx* c)
 {
     Table t;
     t.coef = c->coef.p;
+    t.coef_ff = c->opt.precision == GCV_MIXED ? c->coef_ff.p : nullptr;
     t.seg_t0 = c->seg_t0.p;
     t.seg_t1 = c->seg_t1.p;
     t.seg_f0 = c->seg_f0.p;
@@ -381,7 +382,14 @@ gcv_status to_host(const T* src, size_t n, int where, std::vector<T>& dst)
 gcv_status ensure_table_buffers(gcv_ctx* c)
 {
     const size_t ns = (size_t)std::max<int64_t>(c->n_seg, 1);
-    CHECK(c->coef.reserve((size_t)std::max<int64_t>(c->n_coef, 1)));
+    // one copy of the coefficients: FP64, or float-float for the mixed path
+    if (c->opt.precision == GCV_MIXED) {
+        c->coef.release();
+        CHECK(c->coef_ff.reserve((size_t)std::max<int64_t>(c->n_coef, 1)));
+    } else {
+        c->coef_ff.release();
+        CHECK(c->coef.reserve((size_t)std::max<int64_t>(c->n_coef, 1)));
+    }
     CHECK(c->seg_t0.reserve(ns));
     CHECK(c->seg_t1.reserve(ns));
     CHECK(c->seg_f0.reserve(ns));
@@ -470,7 +478,6 @@ gcv_status build_table(gcv_ctx* c)
 {
     CHECK(ensure_table_buffers(c));
     const bool mixed = c->opt.precision == GCV_MIXED;
-    if (mixed) CHECK(c->coef_ff.reserve((size_t)std::max<int64_t>(c->n_coef, 1)));
     const Batch b = batch_view(c);
     const int setup_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 64));
     CU(cudaEventRecord(c->ev[0], c->stream));
@@ -479,12 +486,6 @@ gcv_status build_table(gcv_ctx* c)
         k_setup<<<setup_blocks, 256, 0, c->stream>>>(b, table_view(c));
         CU(cudaGetLastError());
         c->stats.n_launches++;
-        if (mixed) {
-            const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_coef + 255) / 256, (int64_t)sm_count() * 64));
-            k_coef_ff<<<blocks, 256, 0, c->stream>>>(c->coef.p, c->coef_ff.p, c->n_coef);
-            CU(cudaGetLastError());
-            c->stats.n_launches++;
-        }
     }
     CU(cudaEventRecord(c->ev[1], c->stream));
     for (int attempt = 0;; ++attempt) {

@@ -96,13 +96,14 @@ constexpr int CODE_ELLIPSE = 0;
 __host__ __device__ constexpr int bs_code(int p, int d) { return 16 + 4 * p + d; }
 __host__ __device__ constexpr int code_degree(int code) { return code == 0 ? 0 : (code - 16) / 4; }
 __host__ __device__ constexpr int code_dim(int code) { return code == 0 ? 2 : (code - 16) % 4; }
-// doubles of coefficient data per segment
+// values of coefficient data per segment: the position polynomial of a
+// B-spline piece ((p + 1) D), the 8 ellipse terms
 __host__ __device__ constexpr int code_stride(int code)
 {
-    return code == 0 ? 8 : (2 * code_degree(code) + 1) * code_dim(code);
+    return code == 0 ? 8 : (code_degree(code) + 1) * code_dim(code);
 }
 constexpr int MAX_DEGREE = 5;
-constexpr int MAX_COEF = 33;  // (2*5+1)*3
+constexpr int MAX_COEF = 18;  // (5 + 1) * 3
 
 // Exact 2^-k for 0 <= k <= 1000 built from the exponent bits (no FP64 op).
 __device__ __forceinline__ double pow2_neg(int k)
@@ -188,7 +189,8 @@ struct Eval {
     static constexpr int P = code_degree(CODE);
     static constexpr int D = code_dim(CODE);
     static constexpr int NL = CODE == 0 ? 2 : P * D;  // doubles the speed needs
-    // loads what speed() needs (derivative polynomial / ellipse A, B)
+    // loads what speed() needs: ellipse A, B, or the derivative polynomial
+    // b[k][d] = (k + 1) a[k + 1][d] of the stored position polynomial a
     __device__ __forceinline__ static void load_speed(const double* __restrict__ seg, double* r)
     {
         if constexpr (CODE == 0) {
@@ -196,7 +198,9 @@ struct Eval {
             r[1] = seg[1];
         } else {
 #pragma unroll
-            for (int i = 0; i < P * D; ++i) r[i] = seg[(P + 1) * D + i];
+            for (int k = 0; k < P; ++k)
+#pragma unroll
+                for (int d = 0; d < D; ++d) r[k * D + d] = double(k + 1) * seg[(k + 1) * D + d];
         }
     }
     __device__ __forceinline__ static double speed(const double* r, double v)
@@ -288,8 +292,8 @@ __device__ __forceinline__ void point_dyn(int code, const double* __restrict__ s
 // b_spline_derv_o1 / to_point) run on polynomials in v instead of numbers,
 // with u = m + w v, m the span midpoint and w its half width.  The
 // denominators right[r+1] + left[j-r] are knot differences and do not depend
-// on u.  Output: a[k][d], k = 0..P (position) followed by
-// b[k][d] = (k + 1) a[k + 1][d] (derivative dC/dv).
+// on u.  Output: the position polynomial a[k][d], k = 0..P; the derivative
+// dC/dv is b[k][d] = (k + 1) a[k + 1][d] (see Eval::load_speed).
 template <int P, int D>
 __device__ void bspline_setup(const double* __restrict__ kv, const double* __restrict__ cp, int span,
                               double* out)
@@ -342,10 +346,6 @@ __device__ void bspline_setup(const double* __restrict__ kv, const double* __res
             out[k * D + d] = k == 0 ? acc + q : acc;
         }
     }
-#pragma unroll
-    for (int k = 0; k < P; ++k)
-#pragma unroll
-        for (int d = 0; d < D; ++d) out[(P + 1) * D + k * D + d] = double(k + 1) * out[(k + 1) * D + d];
 }
 
 // ------------------------------------------------------------ warp helpers

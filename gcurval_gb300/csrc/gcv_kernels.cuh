@@ -39,7 +39,8 @@ enum Counter {
 enum ErrBits { ERR_POOL = 1, ERR_SCAN_TIMEOUT = 2, ERR_BAD_KNOTS = 4, ERR_DEEP_LIST = 8 };
 
 struct Table {
-    double* coef;      // per-segment evaluation data (code_stride doubles)
+    double* coef;      // per-segment evaluation data (code_stride doubles), FP64 path
+    float2* coef_ff;   // the same as float-float pairs (mixed path; NULL otherwise)
     double* seg_t0;    // curve parameter at v = -1
     double* seg_t1;    // curve parameter at v = +1
     double* seg_f0;    // f(-1)
@@ -76,47 +77,62 @@ __device__ __forceinline__ void raise_err(const Table& t, unsigned bits)
 // ---------------------------------------------------------------- set-up
 // One thread per segment: segment -> curve map consumer; writes the
 // evaluation data of the segment (B-spline polynomials or ellipse terms).
+// stores a segment's coefficients: FP64, or float-float (hi, lo) pairs when
+// the table is built for the mixed path
+template <int N>
+__device__ __forceinline__ void store_coef(const Table& t, int64_t at, const double* cf)
+{
+    if (t.coef_ff) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            const float h = __double2float_rn(cf[i]);
+            t.coef_ff[at + i] = make_float2(h, __double2float_rn(cf[i] - (double)h));
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) t.coef[at + i] = cf[i];
+    }
+}
+
 template <int P, int D>
 __device__ void setup_bspline_seg(const Batch& b, const Table& t, int64_t s, int64_t c)
 {
+    constexpr int N = code_stride(bs_code(P, D));
     const int64_t j = s - b.seg_off[c];
     const double* kv = b.knots + b.knot_off[c];
     const double* cp = b.ctrl + b.ctrl_off[c];
     const int span = int(j) + P;
-    double* out = t.coef + b.coef_off[c] + j * code_stride(bs_code(P, D));
+    const int64_t at = b.coef_off[c] + j * N;
     const double ka = kv[span], kb = kv[span + 1];
     if (!(kb >= ka)) raise_err(t, ERR_BAD_KNOTS);
+    double cf[N];
     if (kb > ka) {
-        bspline_setup<P, D>(kv, cp, span, out);
+        bspline_setup<P, D>(kv, cp, span, cf);
         t.seg_t0[s] = ka;
         t.seg_t1[s] = kb;
-        double q0;
-        t.seg_f0[s] = Eval<bs_code(P, D)>::speed_slope(out + (P + 1) * D, -1.0, q0);
+        double r[P * D], q0;
+        Eval<bs_code(P, D)>::load_speed(cf, r);
+        t.seg_f0[s] = Eval<bs_code(P, D)>::speed_slope(r, -1.0, q0);
         t.seg_q0[s] = q0;
     } else {
-        for (int i = 0; i < code_stride(bs_code(P, D)); ++i) out[i] = 0.0;
+#pragma unroll
+        for (int i = 0; i < N; ++i) cf[i] = 0.0;
         t.seg_t0[s] = ka;
         t.seg_t1[s] = ka;
         t.seg_f0[s] = 0.0;
         t.seg_q0[s] = 0.0;
     }
+    store_coef<N>(t, at, cf);
 }
 
 __device__ inline void setup_ellipse_seg(const Batch& b, const Table& t, int64_t s, int64_t c)
 {
     const double* e = b.ctrl + b.ctrl_off[c];
-    double* out = t.coef + b.coef_off[c];
     const double a = e[0], bb = e[1];
     double sr, cr;
     sincos(e[2], &sr, &cr);
-    out[0] = a * a - bb * bb;
-    out[1] = bb * bb;
-    out[2] = a;
-    out[3] = bb;
-    out[4] = cr;
-    out[5] = sr;
-    out[6] = e[3];
-    out[7] = e[4];
+    const double out[8] = {a * a - bb * bb, bb * bb, a, bb, cr, sr, e[3], e[4]};
+    store_coef<8>(t, b.coef_off[c], out);
     t.seg_t0[s] = 0.0;
     t.seg_t1[s] = 2.0 * PI;
     t.seg_f0[s] = PI * fabs(bb);

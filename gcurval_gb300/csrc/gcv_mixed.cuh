@@ -86,7 +86,8 @@ template <int CODE>
 struct EvalFF {
     static constexpr int P = code_degree(CODE);
     static constexpr int D = code_dim(CODE);
-    // derivative polynomial (B-spline) or A, B (ellipse) as float-float
+    // A, B (ellipse) or the derivative polynomial b[k][d] = (k + 1) a[k + 1][d]
+    // of the stored float-float position polynomial a
     __device__ __forceinline__ static void load(const float2* __restrict__ seg, ff* r)
     {
         if constexpr (CODE == 0) {
@@ -94,10 +95,12 @@ struct EvalFF {
             r[1] = ff{seg[1].x, seg[1].y};
         } else {
 #pragma unroll
-            for (int i = 0; i < P * D; ++i) {
-                const float2 c = seg[(P + 1) * D + i];
-                r[i] = ff{c.x, c.y};
-            }
+            for (int k = 0; k < P; ++k)
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    const float2 c = seg[(k + 1) * D + d];
+                    r[k * D + d] = k == 0 ? ff{c.x, c.y} : ff_mul_f(ff{c.x, c.y}, float(k + 1));
+                }
         }
     }
     __device__ __forceinline__ static ff speed(const ff* r, ff v)
@@ -227,16 +230,6 @@ __device__ __forceinline__ ff speed_slope_ff_of(int code, const ff* r, ff v, flo
 #undef GCV_CASE
         default: q = 0.0f; return ff{0.0f, 0.0f};
         }
-    }
-}
-
-// float-float copy of every segment's evaluation data (same indexing as coef)
-static __global__ void k_coef_ff(const double* __restrict__ coef, float2* __restrict__ out, int64_t n)
-{
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double x = coef[i];
-        const float h = __double2float_rn(x);
-        out[i] = make_float2(h, __double2float_rn(x - (double)h));
     }
 }
 
@@ -414,11 +407,15 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) k_sample_ff(SampleParams P, co
         } else {
             double p3[3] = {0.0, 0.0, 0.0};
             if (s >= 0) {
-                const double* seg = t.coef + b.coef_off[c] + (s - s0) * code_stride(code);
+                // points from the float-float coefficients, evaluated in FP64
+                const float2* seg = coef_ff + b.coef_off[c] + (s - s0) * code_stride(code);
+                double cd[MAX_COEF];
+                const int n = code_stride(code);
+                for (int k = 0; k < n; ++k) cd[k] = (double)seg[k].x + (double)seg[k].y;
                 if constexpr (CODE >= 0)
-                    Eval<(CODE >= 0 ? CODE : 0)>::point(seg, v, p3);
+                    Eval<(CODE >= 0 ? CODE : 0)>::point(cd, v, p3);
                 else
-                    point_dyn(code, seg, v, p3);
+                    point_dyn(code, cd, v, p3);
             }
             for (int k = 0; k < P.pdim; ++k) P.out[i * P.pdim + k] = p3[k];
         }

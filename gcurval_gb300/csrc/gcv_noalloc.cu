@@ -146,9 +146,10 @@ __global__ void __launch_bounds__(128) k_noalloc_intervals(int n_curve, const in
         if (!(kb >= ka)) {
             atomicOr(reinterpret_cast<unsigned long long*>(scratch), (unsigned long long)ERR_BAD_KNOTS);
         } else if (kb > ka) {
-            double cf[(2 * P + 1) * D];
+            double cf[(P + 1) * D], der[P * D];
             bspline_setup<P, D>(kv, cp, span, cf);
-            len = interval_length<bs_code(P, D)>(cf + (P + 1) * D, rtol, max_depth, &capped);
+            Eval<bs_code(P, D)>::load_speed(cf, der);
+            len = interval_length<bs_code(P, D)>(der, rtol, max_depth, &capped);
         }
         scratch[HEADER_DOUBLES + s] = len;
     }

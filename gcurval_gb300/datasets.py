@@ -95,11 +95,15 @@ class CurveBatch:
 def uniform_positions(n_samples: np.ndarray) -> np.ndarray:
     """Relative positions j / (n - 1), j = 0..n-1, for each curve (0 when n == 1)."""
     n_samples = np.asarray(n_samples, dtype=np.int64)
-    total = int(n_samples.sum())
     off = np.concatenate([[0], np.cumsum(n_samples)])
-    j = np.arange(total, dtype=np.int64) - np.repeat(off[:-1], n_samples)
-    den = np.repeat(np.maximum(n_samples - 1, 1), n_samples).astype(np.float64)
-    return j.astype(np.float64) / den
+    out = np.empty(int(off[-1]))
+    step = 1 << 16
+    for i in range(0, n_samples.size, step):
+        ns = n_samples[i:i + step]
+        lo, hi = int(off[i]), int(off[min(i + step, n_samples.size)])
+        j = np.arange(hi - lo, dtype=np.float64) - np.repeat((off[i:i + ns.size] - lo).astype(np.float64), ns)
+        out[lo:hi] = j / np.repeat(np.maximum(ns - 1, 1).astype(np.float64), ns)
+    return out
 
 
 def _pack(kind, degree, dim, knot_lists_len, knots, ctrl_len, ctrl, n_samples, name, rtol):
@@ -171,61 +175,61 @@ def _segmented_sorted_uniform(rng, counts: np.ndarray) -> np.ndarray:
     return val[keep]
 
 
-def _random_knot_bsplines(rng, degree, dim, n_ctrl, step_sigma, dup_frac=0.0, dup_gap=1e-6):
-    """Clamped B-splines with sorted-uniform interior knots; per-curve degree/dim/n_ctrl arrays."""
-    n = degree.size
+def _ragged_index(starts, lengths):
+    """Flat indices starts[i] + 0..lengths[i]-1 for every i, concatenated."""
+    lengths = np.asarray(lengths, np.int64)
+    tot = int(lengths.sum())
+    if tot == 0:
+        return np.zeros(0, np.int64)
+    first = np.concatenate([[0], np.cumsum(lengths)[:-1]])
+    return np.repeat(np.asarray(starts, np.int64) - first, lengths) + np.arange(tot, dtype=np.int64)
+
+
+_CHUNK = 1 << 16
+
+
+def _bspline_chunk(rng, degree, dim, n_ctrl, step_sigma, dup_frac, dup_gap):
     n_int = n_ctrl - degree - 1
     inner = _segmented_sorted_uniform(rng, n_int)
-    if dup_frac > 0.0 and inner.size:
-        # 5 % of interior knots become previous + gap (near-duplicate knots)
-        io = np.concatenate([[0], np.cumsum(n_int)])
-        first = np.zeros(inner.size, bool)
-        first[io[:-1][n_int > 0]] = True
-        pick = (rng.random(inner.size) < dup_frac) & ~first
-        idx = np.nonzero(pick)[0]
-        inner[idx] = np.minimum(inner[idx - 1] + dup_gap, 1.0)
-        # keep each curve's interior sorted after the replacements
-        order = np.lexsort((inner, np.repeat(np.arange(n), n_int)))
-        inner = inner[order]
-    n_knots = n_ctrl + degree + 1
-    total_k = int(n_knots.sum())
-    knots = np.empty(total_k)
-    ko = np.concatenate([[0], np.cumsum(n_knots)])
     io = np.concatenate([[0], np.cumsum(n_int)])
-    # vectorised fill: position within curve
-    cid = np.repeat(np.arange(n), n_knots)
-    j = np.arange(total_k) - ko[cid]
-    p = degree[cid]
-    lo = j <= p
-    hi = j >= (n_ctrl[cid])
-    mid = ~(lo | hi)
-    knots[lo] = 0.0
-    knots[hi] = 1.0
-    knots[mid] = inner[io[cid[mid]] + (j[mid] - p[mid] - 1)]
-    # control points: random walk per curve, dim per curve
-    clen = n_ctrl * dim
-    tot_c = int(clen.sum())
-    steps = rng.normal(0.0, step_sigma, tot_c)
-    co = np.concatenate([[0], np.cumsum(clen)])
-    # zero the first point of each curve, cumulative sum per (curve, axis)
-    ccid = np.repeat(np.arange(n), clen)
-    k = np.arange(tot_c) - co[ccid]
-    d = dim[ccid].astype(np.int64)
-    axis = k % d
-    first = k < d
-    steps[first] = 0.0
-    # segmented cumsum along each (curve, axis) stream: reorder to axis-major within curve
-    key = ccid * 3 + axis
-    order = np.lexsort((k, key))
-    s = steps[order]
-    cs = np.cumsum(s)
-    keys_sorted = key[order]
-    starts = np.r_[0, np.nonzero(np.diff(keys_sorted))[0] + 1]
-    grp = np.repeat(np.arange(starts.size), np.diff(np.r_[starts, s.size]))
-    offs = np.r_[0.0, cs][starts][grp]
-    ctrl = np.empty(tot_c)
-    ctrl[order] = cs - offs
-    return n_knots, knots, clen, ctrl
+    if dup_frac > 0.0 and inner.size:
+        # a fraction of the interior knots become previous + gap (near-duplicate
+        # knots); min() with the next knot keeps every curve's interior sorted
+        has = n_int > 0
+        first = np.zeros(inner.size, bool)
+        first[io[:-1][has]] = True
+        nxt = np.append(inner[1:], 1.0)
+        nxt[io[1:][has] - 1] = 1.0
+        pick = np.nonzero((rng.random(inner.size) < dup_frac) & ~first)[0]
+        inner[pick] = np.minimum(inner[pick - 1] + dup_gap, nxt[pick])
+    n_knots = n_ctrl + degree + 1
+    ko = np.concatenate([[0], np.cumsum(n_knots)])
+    knots = np.ones(int(ko[-1]))
+    knots[_ragged_index(ko[:-1], degree + 1)] = 0.0
+    knots[_ragged_index(ko[:-1] + degree + 1, n_int)] = inner
+    # control points: random walk from the origin, one (x, y, z) row per point,
+    # z dropped for 2D curves
+    po = np.concatenate([[0], np.cumsum(n_ctrl)])
+    steps = rng.normal(0.0, step_sigma, (int(po[-1]), 3))
+    steps[po[:-1]] = 0.0
+    cs = np.cumsum(steps, axis=0)
+    cs -= np.repeat(cs[po[:-1]], n_ctrl, axis=0)
+    keep = np.arange(3)[None, :] < np.repeat(dim, n_ctrl)[:, None]
+    return n_knots, knots, n_ctrl * dim, cs[keep]
+
+
+def _random_knot_bsplines(rng, degree, dim, n_ctrl, step_sigma, dup_frac=0.0, dup_gap=1e-6):
+    """Clamped B-splines with sorted-uniform interior knots and random-walk control
+    points; per-curve degree / dim / n_ctrl arrays.  Linear time, in chunks of
+    curves, so that a million curves with hundreds of millions of knots fit."""
+    degree = np.asarray(degree, np.int64)
+    dim = np.asarray(dim, np.int64)
+    n_ctrl = np.asarray(n_ctrl, np.int64)
+    parts = [_bspline_chunk(rng, degree[i:i + _CHUNK], dim[i:i + _CHUNK], n_ctrl[i:i + _CHUNK], step_sigma,
+                            dup_frac, dup_gap) for i in range(0, degree.size, _CHUNK)]
+    if not parts:
+        return np.zeros(0, np.int64), np.zeros(0), np.zeros(0, np.int64), np.zeros(0)
+    return tuple(np.concatenate([p[k] for p in parts]) for k in range(4))
 
 
 def mixed3d_bsplines(n: int = 100_000, n_samples: int = 2048, seed: int = 0, rtol: float = 1e-8) -> CurveBatch:
@@ -251,36 +255,40 @@ def uneven_batch(n: int = 1_000_000, seed: int = 0, rtol: float = 1e-8,
     degree = rng.integers(2, 6, nb).astype(np.int64)
     dim = rng.integers(2, 4, nb).astype(np.int64)
     n_ctrl = np.maximum(_log_uniform_int(rng, 4, max_ctrl, nb), degree + 1)
-    n_knots_b, knots_b, clen_b, ctrl_b = _random_knot_bsplines(rng, degree, dim, n_ctrl, 1.0, dup_frac=0.05)
     prm = _ellipse_params(rng, ne)
     n_samp = _log_uniform_int(rng, min_samples, max_samples, n)
-    # interleave ellipses and B-splines in curve order
     kind = np.where(is_ell, KIND_ELLIPSE, KIND_BSPLINE)
     deg = np.zeros(n, np.int64)
     dm = np.full(n, 2, np.int64)
     deg[~is_ell] = degree
     dm[~is_ell] = dim
-    klen = np.full(n, 2, np.int64)
-    klen[~is_ell] = n_knots_b
-    clen = np.full(n, 5, np.int64)
-    clen[~is_ell] = clen_b
-    ko = np.concatenate([[0], np.cumsum(klen)])
-    co = np.concatenate([[0], np.cumsum(clen)])
-    knots = np.empty(int(ko[-1]))
-    ctrl = np.empty(int(co[-1]))
-    # ellipse parts
-    e_idx = np.nonzero(is_ell)[0]
-    knots[ko[e_idx]] = 0.0
-    knots[ko[e_idx] + 1] = TWO_PI
-    ctrl[(co[e_idx][:, None] + np.arange(5)).reshape(-1)] = prm.reshape(-1)
-    # B-spline parts (copy contiguous runs)
-    b_idx = np.nonzero(~is_ell)[0]
-    kb_off = np.concatenate([[0], np.cumsum(n_knots_b)])
-    cb_off = np.concatenate([[0], np.cumsum(clen_b)])
-    dst_k = np.repeat(ko[b_idx], n_knots_b) + (np.arange(kb_off[-1]) - np.repeat(kb_off[:-1], n_knots_b))
-    knots[dst_k] = knots_b
-    dst_c = np.repeat(co[b_idx], clen_b) + (np.arange(cb_off[-1]) - np.repeat(cb_off[:-1], clen_b))
-    ctrl[dst_c] = ctrl_b
+    nc = np.zeros(n, np.int64)
+    nc[~is_ell] = n_ctrl
+    ell_prm = np.zeros((n, 5))
+    ell_prm[is_ell] = prm
+    klen = np.where(is_ell, 2, nc + deg + 1)
+    clen = np.where(is_ell, 5, nc * dm)
+    # B-spline data in chunks of curves, interleaved with the ellipses in curve order
+    knots_parts, ctrl_parts = [], []
+    for i in range(0, n, _CHUNK):
+        sl = slice(i, min(i + _CHUNK, n))
+        e = is_ell[sl]
+        b = ~e
+        nk, kb, cl, cb = _bspline_chunk(rng, deg[sl][b], dm[sl][b], nc[sl][b], 1.0, 0.05, 1e-6)
+        ko = np.concatenate([[0], np.cumsum(klen[sl])])
+        co = np.concatenate([[0], np.cumsum(clen[sl])])
+        kn = np.empty(int(ko[-1]))
+        ct = np.empty(int(co[-1]))
+        kn[_ragged_index(ko[:-1][b], nk)] = kb
+        ct[_ragged_index(co[:-1][b], cl)] = cb
+        ei = np.nonzero(e)[0]
+        kn[ko[ei]] = 0.0
+        kn[ko[ei] + 1] = TWO_PI
+        ct[_ragged_index(co[ei], np.full(ei.size, 5))] = ell_prm[sl][e].reshape(-1)
+        knots_parts.append(kn)
+        ctrl_parts.append(ct)
+    knots = np.concatenate(knots_parts) if knots_parts else np.zeros(0)
+    ctrl = np.concatenate(ctrl_parts) if ctrl_parts else np.zeros(0)
     return _pack(kind, deg, dm, klen, knots, clen, ctrl, n_samp, "uneven_batch", rtol)
 
 
