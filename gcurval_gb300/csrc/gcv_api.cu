@@ -110,6 +110,11 @@ int sm_count()
 
 }  // namespace
 
+struct CodeRange {
+    int code;
+    int64_t begin, end;  // range of the grouped segment list
+};
+
 struct gcv_ctx {
     gcv_options opt{};
     cudaStream_t stream = nullptr;
@@ -127,6 +132,9 @@ struct gcv_ctx {
     std::vector<int64_t> h_seg_off;
     std::vector<uint8_t> h_kind, h_degree;
     std::vector<double> h_start;  // first parameter value of each curve
+    // batches that mix curve codes: segments grouped by code, one range per code
+    DBuf<int> seg_list;
+    std::vector<CodeRange> code_ranges;
 
     // table
     DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_q0, seg_len, seg_cum, curve_len;
@@ -228,6 +236,7 @@ void destroy_ctx(gcv_ctx* c)
     c->seg_off.release();
     c->coef_off.release();
     c->seg_curve.release();
+    c->seg_list.release();
     c->coef.release();
     c->seg_t0.release();
     c->seg_t1.release();
@@ -279,7 +288,7 @@ gcv_status derive_layout(gcv_ctx* c, const uint8_t* kind, const uint8_t* degree,
         if (kind[i] == GCV_KIND_ELLIPSE) {
             if (nk != 2 || nc != 5)
                 return fail(GCV_ERR_INVALID, "curve " + std::to_string(i) + ": an ellipse has 2 knots and 5 control values");
-            ns = 1;
+            ns = ELLIPSE_PIECES;
             code = CODE_ELLIPSE;
         } else if (kind[i] == GCV_KIND_BSPLINE) {
             const int p = degree[i];
@@ -338,6 +347,48 @@ gcv_status finish_create(gcv_ctx* c, const uint8_t* kind, const uint8_t* degree,
         k_seg_curve<<<blocks, 256, 0, c->stream>>>(b, c->seg_curve.p);
         CU(cudaGetLastError());
         c->stats.n_launches++;
+    }
+    if (c->code < 0 && c->n_seg > 0) {
+        // Group the segments by curve code (stable within a code), so that
+        // every main-pass launch runs one specialised kernel over one code.
+        const int64_t n = c->n_curve;
+        std::vector<int> code_of((size_t)n);
+        std::vector<int64_t> per_code(64, 0);
+        for (int64_t i = 0; i < n; ++i) {
+            const int cd = kind[i] == GCV_KIND_ELLIPSE ? CODE_ELLIPSE : bs_code(degree[i], dim[i]);
+            code_of[(size_t)i] = cd;
+            per_code[(size_t)cd] += seg_off[(size_t)i + 1] - seg_off[(size_t)i];
+        }
+        std::vector<int64_t> base(64, 0);
+        int64_t at = 0;
+        c->code_ranges.clear();
+        for (int cd = 0; cd < 64; ++cd) {
+            base[(size_t)cd] = at;
+            if (per_code[(size_t)cd] > 0) {
+                c->code_ranges.push_back(CodeRange{cd, at, at + per_code[(size_t)cd]});
+                at += per_code[(size_t)cd];
+            }
+        }
+        if (c->code_ranges.size() > (size_t)(C_COUNT - C_WORK_CODE))
+            return fail(GCV_ERR_INVALID, "too many distinct curve codes in one batch");
+        std::vector<int64_t> dst((size_t)n);
+        for (int64_t i = 0; i < n; ++i) {
+            int64_t& nb = base[(size_t)code_of[(size_t)i]];
+            dst[(size_t)i] = nb;
+            nb += seg_off[(size_t)i + 1] - seg_off[(size_t)i];
+        }
+        DBuf<int64_t> d_dst;
+        struct Release {
+            DBuf<int64_t>& b;
+            ~Release() { b.release(); }
+        } release_dst{d_dst};
+        CHECK(upload(d_dst, dst.data(), dst.size(), c->stream));
+        CHECK(c->seg_list.reserve((size_t)c->n_seg));
+        const int blocks = (int)std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 32);
+        k_group_segments<<<blocks, 256, 0, c->stream>>>(batch_view(c), d_dst.p, c->seg_list.p);
+        CU(cudaGetLastError());
+        c->stats.n_launches++;
+        CU(cudaStreamSynchronize(c->stream));
     }
     CU(cudaStreamSynchronize(c->stream));
     c->stats.n_curves = c->n_curve;
@@ -400,13 +451,15 @@ gcv_status ensure_table_buffers(gcv_ctx* c)
     CHECK(c->leaf_cnt.reserve(ns));
     CHECK(c->curve_len.reserve((size_t)std::max<int64_t>(c->n_curve, 1)));
     if (c->leaf_cap == 0) {
-        c->leaf_cap = 2 * (int64_t)ns + 4096;
+        // about three leaves per interval at the default tolerances; a pool
+        // that turns out short sends the rest to the deep passes, which grow it
+        c->leaf_cap = 3 * (int64_t)ns + 4096;
         CHECK(c->leaf_v.reserve((size_t)c->leaf_cap));
         CHECK(c->leaf_cum.reserve((size_t)c->leaf_cap));
         CHECK(c->leaf_f.reserve((size_t)c->leaf_cap));
         CHECK(c->leaf_q.reserve((size_t)c->leaf_cap));
     }
-    if (c->deep_list.n == 0) CHECK(c->deep_list.reserve(ns / 64 + 1024));
+    if (c->deep_list.n == 0) CHECK(c->deep_list.reserve(ns / 16 + 1024));
     const size_t tiles = (ns + SCAN_TILE - 1) / SCAN_TILE;
     CHECK(c->scan_status.reserve(tiles));
     CHECK(c->scan_flag.reserve(tiles));
@@ -440,38 +493,61 @@ gcv_status read_counters(gcv_ctx* c)
     return GCV_OK;
 }
 
-template <int MODE, int CODE, int PREC>
-gcv_status launch_length_k(gcv_ctx* c, const LengthParams& P)
+// k_length over P for one curve code: every code has a specialised main
+// pass; the deep passes are specialised for the common uniform batches and
+// dispatch per segment otherwise (their lists mix codes)
+template <int MODE, int PREC>
+gcv_status launch_length_code(gcv_ctx* c, int code, const LengthParams& P)
 {
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, CODE, PREC>, LK_THREADS, 0);
-    if (e != cudaSuccess) return cuda_fail(e, "occupancy query");
-    occ = std::max(1, std::min(occ, 32));
-    // persistent: fill the GPU, but no more lanes than there are intervals
-    const int64_t want = (P.n_items + LK_THREADS - 1) / LK_THREADS;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)sm_count() * occ, want));
-    k_length<MODE, CODE, PREC><<<grid, LK_THREADS, 0, c->stream>>>(P);
-    CU(cudaGetLastError());
+    const int sms = sm_count();
+    cudaError_t e = cudaErrorInvalidValue;
+    if constexpr (MODE == 0) {
+        switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: e = length_launch<0, C, PREC>(P, c->stream, sms); break;
+            GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+        default: return fail(GCV_ERR_INVALID, "no length kernel for curve code " + std::to_string(code));
+        }
+    } else {
+        switch (code) {
+        case CODE_ELLIPSE: e = length_launch<MODE, CODE_ELLIPSE, PREC>(P, c->stream, sms); break;
+        case bs_code(3, 2): e = length_launch<MODE, bs_code(3, 2), PREC>(P, c->stream, sms); break;
+        case bs_code(3, 3): e = length_launch<MODE, bs_code(3, 3), PREC>(P, c->stream, sms); break;
+        default: e = length_launch<MODE, -1, PREC>(P, c->stream, sms); break;
+        }
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "length kernel launch");
     c->stats.n_launches++;
     return GCV_OK;
 }
 
-// specialised kernels for the common uniform batches, the runtime dispatch otherwise
-template <int MODE, int PREC>
-gcv_status launch_length_p(gcv_ctx* c, const LengthParams& P)
+template <int MODE>
+gcv_status launch_length(gcv_ctx* c, int code, const LengthParams& P)
 {
-    switch (c->code) {
-    case CODE_ELLIPSE: return launch_length_k<MODE, CODE_ELLIPSE, PREC>(c, P);
-    case bs_code(3, 2): return launch_length_k<MODE, bs_code(3, 2), PREC>(c, P);
-    case bs_code(3, 3): return launch_length_k<MODE, bs_code(3, 3), PREC>(c, P);
-    default: return launch_length_k<MODE, -1, PREC>(c, P);
-    }
+    return c->opt.precision == GCV_MIXED ? launch_length_code<MODE, 1>(c, code, P)
+                                         : launch_length_code<MODE, 0>(c, code, P);
 }
 
-template <int MODE>
-gcv_status launch_length(gcv_ctx* c, const LengthParams& P)
+// Main pass: one launch over all segments of a uniform batch, or one launch
+// per curve code over that code's range of the grouped segment list.
+gcv_status launch_main_pass(gcv_ctx* c, LengthParams P)
 {
-    return c->opt.precision == GCV_MIXED ? launch_length_p<MODE, 1>(c, P) : launch_length_p<MODE, 0>(c, P);
+    if (c->code >= 0) {
+        P.list = nullptr;
+        P.n_items = c->n_seg;
+        P.work = c->ctr.p + C_WORK;
+        return launch_length<0>(c, c->code, P);
+    }
+    for (size_t k = 0; k < c->code_ranges.size(); ++k) {
+        const CodeRange& r = c->code_ranges[k];
+        if (r.end == r.begin) continue;
+        P.list = c->seg_list.p + r.begin;
+        P.n_items = r.end - r.begin;
+        P.work = c->ctr.p + C_WORK_CODE + k;
+        CHECK(launch_length<0>(c, r.code, P));
+    }
+    return GCV_OK;
 }
 
 gcv_status build_table(gcv_ctx* c)
@@ -489,9 +565,10 @@ gcv_status build_table(gcv_ctx* c)
     }
     CU(cudaEventRecord(c->ev[1], c->stream));
     for (int attempt = 0;; ++attempt) {
-        if (attempt > 8) return fail(GCV_ERR_OVERFLOW, "leaf pool kept overflowing");
+        if (attempt > 8) return fail(GCV_ERR_OVERFLOW, "deep list kept overflowing");
         // keep the set-up's error bits, clear the rest
         CU(cudaMemsetAsync(c->ctr.p, 0, C_ERR * sizeof(unsigned long long), c->stream));
+        CU(cudaMemsetAsync(c->ctr.p + C_WORK_CODE, 0, (C_COUNT - C_WORK_CODE) * sizeof(unsigned long long), c->stream));
         LengthParams P;
         P.b = b;
         P.t = table_view(c);
@@ -500,17 +577,13 @@ gcv_status build_table(gcv_ctx* c)
         P.max_depth = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
         P.collect = c->opt.collect_stats;
         P.list = nullptr;
-        P.n_items = c->n_seg;
+        P.n_items = 0;
         P.coef_ff = c->coef_ff.p;
-        if (c->n_seg > 0) CHECK(launch_length<0>(c, P));
+        P.work = c->ctr.p + C_WORK;
+        if (c->n_seg > 0) CHECK(launch_main_pass(c, P));
         CHECK(read_counters(c));
         const unsigned long long err = c->h_ctr[C_ERR];
         if (err & ERR_BAD_KNOTS) return fail(GCV_ERR_INVALID, "knot vector decreases or holds NaN");
-        if (err & ERR_POOL) {
-            CHECK(grow_pool(c, (int64_t)(c->h_ctr[C_LEAF_TOP] * 1.25) + 4096, 0));
-            CU(cudaMemsetAsync(c->ctr.p + C_ERR, 0, sizeof(unsigned long long), c->stream));
-            continue;
-        }
         if (err & ERR_DEEP_LIST) {
             DBuf<int>& dl = c->deep_list;
             const size_t need = (size_t)(c->h_ctr[C_DEEP] * 1.25) + 1024;
@@ -520,29 +593,33 @@ gcv_status build_table(gcv_ctx* c)
             continue;
         }
         const int64_t n_deep = (int64_t)c->h_ctr[C_DEEP];
-        int64_t top = (int64_t)c->h_ctr[C_LEAF_TOP];
+        // Intervals whose leaves did not fit the pool went to the deep list;
+        // what was reserved past the pool's end holds nothing.
+        int64_t top = std::min<int64_t>((int64_t)c->h_ctr[C_LEAF_TOP], c->leaf_cap);
         if (n_deep > 0) {
-            // count pass
+            unsigned long long top_u = (unsigned long long)top;
+            CU(cudaMemcpyAsync(c->ctr.p + C_LEAF_TOP, &top_u, sizeof(top_u), cudaMemcpyHostToDevice, c->stream));
+            // count pass, then the leaves of the whole list summed on the device
             CU(cudaMemsetAsync(c->ctr.p + C_WORK, 0, sizeof(unsigned long long), c->stream));
+            CU(cudaMemsetAsync(c->ctr.p + C_DEEP_LEAVES, 0, sizeof(unsigned long long), c->stream));
             LengthParams Q = P;
             Q.t = table_view(c);
             Q.list = c->deep_list.p;
             Q.n_items = n_deep;
             Q.collect = 0;
-            CHECK(launch_length<1>(c, Q));
-            // total leaves of the deep segments: sum leaf_cnt over the list
-            std::vector<int> ids((size_t)n_deep);
-            CU(cudaMemcpyAsync(ids.data(), c->deep_list.p, (size_t)n_deep * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-            std::vector<int> cnt((size_t)c->n_seg);
-            CU(cudaMemcpyAsync(cnt.data(), c->leaf_cnt.p, (size_t)c->n_seg * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-            CU(cudaStreamSynchronize(c->stream));
-            int64_t extra = 0;
-            for (int s : ids) extra += cnt[(size_t)s];
-            if (top + extra > c->leaf_cap) CHECK(grow_pool(c, top + extra + 4096, top));
+            Q.work = c->ctr.p + C_WORK;
+            CHECK(launch_length<1>(c, c->code, Q));
+            const int rb = (int)std::min<int64_t>((n_deep + 255) / 256, (int64_t)sm_count() * 8);
+            k_deep_total<<<rb, 256, 0, c->stream>>>(c->deep_list.p, n_deep, c->leaf_cnt.p, c->ctr.p + C_DEEP_LEAVES);
+            CU(cudaGetLastError());
+            c->stats.n_launches++;
+            CHECK(read_counters(c));
+            const int64_t extra = (int64_t)c->h_ctr[C_DEEP_LEAVES];
+            if (top + extra > c->leaf_cap) CHECK(grow_pool(c, top + extra + (top + extra) / 16 + 4096, top));
             CU(cudaMemsetAsync(c->ctr.p + C_WORK, 0, sizeof(unsigned long long), c->stream));
             Q.t = table_view(c);
             Q.collect = P.collect;
-            CHECK(launch_length<2>(c, Q));
+            CHECK(launch_length<2>(c, c->code, Q));
             CHECK(read_counters(c));
             if (c->h_ctr[C_ERR] & ERR_POOL) return fail(GCV_ERR_OVERFLOW, "leaf pool overflow in the deep pass");
             top = (int64_t)c->h_ctr[C_LEAF_TOP];

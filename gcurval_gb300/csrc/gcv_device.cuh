@@ -4,7 +4,8 @@
 //
 // Every knot interval ("segment") is mapped to a local variable v in [-1, 1]:
 //   B-spline  t = t0 + (v + 1) * hw,  hw = (k[span+1] - k[span]) / 2
-//   ellipse   theta = pi * (v + 1)   (t0 = 0, hw = pi)
+//   ellipse   piece j of ELLIPSE_PIECES equal parameter pieces of [0, 2 pi]:
+//             theta = pi * (2 j + 1 + v) / ELLIPSE_PIECES
 // and the integrand is f(v) = |dC/dv| = |C'(t)| * hw, so that the segment
 // length is the integral of f over [-1, 1].
 #pragma once
@@ -97,11 +98,16 @@ __host__ __device__ constexpr int bs_code(int p, int d) { return 16 + 4 * p + d;
 __host__ __device__ constexpr int code_degree(int code) { return code == 0 ? 0 : (code - 16) / 4; }
 __host__ __device__ constexpr int code_dim(int code) { return code == 0 ? 2 : (code - 16) % 4; }
 // values of coefficient data per segment: the position polynomial of a
-// B-spline piece ((p + 1) D), the 8 ellipse terms
+// B-spline piece ((p + 1) D), the 9 ellipse terms
 __host__ __device__ constexpr int code_stride(int code)
 {
-    return code == 0 ? 8 : (code_degree(code) + 1) * code_dim(code);
+    return code == 0 ? 9 : (code_degree(code) + 1) * code_dim(code);
 }
+// An ellipse is integrated as this many equal parameter pieces (a power of
+// two, so that v / ELLIPSE_PIECES is exact): more lanes per curve and a few
+// leaves per piece instead of one long chain of panels.
+constexpr int ELLIPSE_PIECES = 8;
+constexpr double ELLIPSE_PIECE_SCALE = 1.0 / ELLIPSE_PIECES;
 constexpr int MAX_DEGREE = 5;
 constexpr int MAX_COEF = 18;  // (5 + 1) * 3
 
@@ -112,13 +118,15 @@ __device__ __forceinline__ double pow2_neg(int k)
 }
 
 // ------------------------------------------------------------- evaluators
-// Ellipse segment data (8 doubles): A = a^2 - b^2, B = b^2, a, b, cos(rot),
-// sin(rot), cx, cy.  f(v) = pi * sqrt(B + A sin^2(pi v)), because
-// |C'(theta)|^2 = a^2 sin^2 + b^2 cos^2 and sin^2(pi (v + 1)) = sin^2(pi v).
-__device__ __forceinline__ double ellipse_speed(double A, double B, double v)
+// Ellipse piece data (9 doubles): A = (a^2 - b^2) h^2, B = b^2 h^2 with
+// h = pi / ELLIPSE_PIECES, w0 = (2 j + 1) / ELLIPSE_PIECES - 1, then a, b,
+// cos(rot), sin(rot), cx, cy.  With w = w0 + v / ELLIPSE_PIECES in [-1, 1]
+// (theta = pi (w + 1)): f(v) = sqrt(B + A sin^2(pi w)), because
+// |C'(theta)|^2 = a^2 sin^2 + b^2 cos^2 and sin^2(pi (w + 1)) = sin^2(pi w).
+__device__ __forceinline__ double ellipse_speed(double A, double B, double w0, double v)
 {
-    const double s = sinpi(v);
-    return PI * sqrt(fma(A * s, s, B));
+    const double s = sinpi(fma(v, ELLIPSE_PIECE_SCALE, w0));
+    return sqrt(fma(A * s, s, B));
 }
 
 // B-spline segment data: position polynomial a[k][d] (k = 0..P), then the
@@ -158,13 +166,14 @@ __device__ __forceinline__ double bs_speed_slope(const double* b, double v, doub
     return sqrt(s);
 }
 
-// ellipse: f^2 = pi^2 (B + A sin^2(pi v)), so q = f f' = pi^3 A sin cos
-__device__ __forceinline__ double ellipse_speed_slope(double A, double B, double v, double& q)
+// ellipse: f^2 = B + A sin^2(pi w), dw/dv = 1 / ELLIPSE_PIECES, so
+// q = f f' = A sin cos pi / ELLIPSE_PIECES
+__device__ __forceinline__ double ellipse_speed_slope(double A, double B, double w0, double v, double& q)
 {
     double s, c;
-    sincospi(v, &s, &c);
-    q = PI * PI * PI * A * s * c;
-    return PI * sqrt(fma(A * s, s, B));
+    sincospi(fma(v, ELLIPSE_PIECE_SCALE, w0), &s, &c);
+    q = (PI * ELLIPSE_PIECE_SCALE) * A * s * c;
+    return sqrt(fma(A * s, s, B));
 }
 
 template <int P, int D>
@@ -188,14 +197,15 @@ template <int CODE>
 struct Eval {
     static constexpr int P = code_degree(CODE);
     static constexpr int D = code_dim(CODE);
-    static constexpr int NL = CODE == 0 ? 2 : P * D;  // doubles the speed needs
-    // loads what speed() needs: ellipse A, B, or the derivative polynomial
+    static constexpr int NL = CODE == 0 ? 3 : P * D;  // doubles the speed needs
+    // loads what speed() needs: ellipse A, B, w0, or the derivative polynomial
     // b[k][d] = (k + 1) a[k + 1][d] of the stored position polynomial a
     __device__ __forceinline__ static void load_speed(const double* __restrict__ seg, double* r)
     {
         if constexpr (CODE == 0) {
             r[0] = seg[0];
             r[1] = seg[1];
+            r[2] = seg[2];
         } else {
 #pragma unroll
             for (int k = 0; k < P; ++k)
@@ -206,7 +216,7 @@ struct Eval {
     __device__ __forceinline__ static double speed(const double* r, double v)
     {
         if constexpr (CODE == 0)
-            return ellipse_speed(r[0], r[1], v);
+            return ellipse_speed(r[0], r[1], r[2], v);
         else
             return bs_speed<P, D>(r, v);
     }
@@ -214,7 +224,7 @@ struct Eval {
     __device__ __forceinline__ static double speed_slope(const double* r, double v, double& q)
     {
         if constexpr (CODE == 0)
-            return ellipse_speed_slope(r[0], r[1], v, q);
+            return ellipse_speed_slope(r[0], r[1], r[2], v, q);
         else
             return bs_speed_slope<P, D>(r, v, q);
     }
@@ -222,11 +232,12 @@ struct Eval {
     __device__ __forceinline__ static void point(const double* __restrict__ seg, double v, double* out)
     {
         if constexpr (CODE == 0) {
+            // theta / pi = (2 j + 1 + v) / ELLIPSE_PIECES = (w0 + 1) + v / ELLIPSE_PIECES
             double s, c;
-            sincospi(v + 1.0, &s, &c);
-            const double x = seg[2] * c, y = seg[3] * s;
-            out[0] = seg[4] * x - seg[5] * y + seg[6];
-            out[1] = seg[5] * x + seg[4] * y + seg[7];
+            sincospi(fma(v, ELLIPSE_PIECE_SCALE, seg[2] + 1.0), &s, &c);
+            const double x = seg[3] * c, y = seg[4] * s;
+            out[0] = seg[5] * x - seg[6] * y + seg[7];
+            out[1] = seg[6] * x + seg[5] * y + seg[8];
         } else {
             double a[(P + 1) * D];
 #pragma unroll

@@ -1,0 +1,226 @@
+// Float-float evaluators of the mixed-precision path: curve speeds in
+// float-float arithmetic (gcv_ff.cuh), an own float-float sin(pi x) for
+// ellipses, and the 15-node Kronrod panel built from them.
+#pragma once
+
+#include "gcv_ff.cuh"
+#include "gcv_table.cuh"
+
+namespace gcv {
+
+// float-float constants from double literals (split at compile time)
+struct ffc {
+    float hi, lo;
+};
+__host__ __device__ constexpr ffc split_const(double x)
+{
+    return ffc{(float)x, (float)(x - (double)(float)x)};
+}
+__device__ __forceinline__ ff to_ff(ffc c) { return ff{c.hi, c.lo}; }
+
+// ------------------------------------------------------- sin(pi x), |x| <= 1
+// Reduce x to r in [-1/4, 1/4] with sin(pi x) = +-sin(pi r) or +-cos(pi r),
+// then Taylor series of sin(t), cos(t) in t = pi r (|t| <= pi/4: the 17th /
+// 16th order terms are below 2e-14, far under float-float rounding).
+__device__ __forceinline__ ff ff_sin_taylor(ff t)
+{
+    const ff t2 = ff_mul(t, t);
+    // t * (1 - t^2/3! + t^4/5! - ... + t^16/17!)
+    ff p = to_ff(split_const(1.0 / 355687428096000.0));  // 1/17!
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 1307674368000.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 6227020800.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 39916800.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 362880.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 5040.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 120.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 6.0))));
+    p = ff_fma(p, t2, ff{1.0f, 0.0f});
+    return ff_mul(p, t);
+}
+__device__ __forceinline__ ff ff_cos_taylor(ff t)
+{
+    const ff t2 = ff_mul(t, t);
+    ff p = to_ff(split_const(1.0 / 20922789888000.0));  // 1/16!
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 87178291200.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 479001600.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 3628800.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 40320.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 720.0))));
+    p = ff_fma(p, t2, to_ff(split_const(1.0 / 24.0)));
+    p = ff_fma(p, t2, ff_neg(to_ff(split_const(0.5))));
+    return ff_fma(p, t2, ff{1.0f, 0.0f});
+}
+
+// sin(pi x)^2 for x in [-1, 1]
+__device__ __forceinline__ ff ff_sinpi_sq(ff x)
+{
+    // sin^2(pi x) has period 1 and is even: fold to y in [0, 1/2]
+    float ax = fabsf(x.hi);
+    ff y = x.hi < 0.0f ? ff_neg(x) : x;
+    if (ax > 0.5f) y = ff_add_f(ff_neg(y), 1.0f);  // 1 - |x|
+    (void)ax;
+    // y in [0, 1/2]: sin(pi y) = cos(pi (1/2 - y)); use sin for y <= 1/4
+    const ff pi = to_ff(split_const(3.141592653589793238462643383279502884));
+    ff s;
+    if (y.hi <= 0.25f) {
+        s = ff_sin_taylor(ff_mul(pi, y));
+    } else {
+        s = ff_cos_taylor(ff_mul(pi, ff_add_f(ff_neg(y), 0.5f)));
+    }
+    return ff_mul(s, s);
+}
+
+// ------------------------------------------------------------- evaluators
+template <int CODE>
+struct EvalFF {
+    static constexpr int P = code_degree(CODE);
+    static constexpr int D = code_dim(CODE);
+    // A, B, w0 (ellipse piece) or the derivative polynomial
+    // b[k][d] = (k + 1) a[k + 1][d] of the stored float-float position polynomial a
+    __device__ __forceinline__ static void load(const float2* __restrict__ seg, ff* r)
+    {
+        if constexpr (CODE == 0) {
+            r[0] = ff{seg[0].x, seg[0].y};
+            r[1] = ff{seg[1].x, seg[1].y};
+            r[2] = ff{seg[2].x, seg[2].y};  // w0 = (2 j + 1) / ELLIPSE_PIECES - 1: exact in FP32
+        } else {
+#pragma unroll
+            for (int k = 0; k < P; ++k)
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    const float2 c = seg[(k + 1) * D + d];
+                    r[k * D + d] = k == 0 ? ff{c.x, c.y} : ff_mul_f(ff{c.x, c.y}, float(k + 1));
+                }
+        }
+    }
+    __device__ __forceinline__ static ff speed(const ff* r, ff v)
+    {
+        if constexpr (CODE == 0) {
+            // sqrt(B + A sin^2(pi w)), w = w0 + v / ELLIPSE_PIECES in [-1, 1]
+            const ff w = ff_add_f(ff_scale(v, (float)ELLIPSE_PIECE_SCALE), r[2].hi);
+            const ff s2 = ff_sinpi_sq(w);
+            return ff_sqrt(ff_fma(r[0], s2, r[1]));
+        } else {
+            ff s{0.0f, 0.0f};
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                ff acc = r[(P - 1) * D + d];
+#pragma unroll
+                for (int k = P - 2; k >= 0; --k) acc = ff_fma(acc, v, r[k * D + d]);
+                s = d == 0 ? ff_mul(acc, acc) : ff_fma(acc, acc, s);
+            }
+            return ff_sqrt(s);
+        }
+    }
+    // speed and q = f * df/dv (q only to FP32 accuracy: it shapes the initial guess
+    // and the stopping test, never the result)
+    __device__ __forceinline__ static ff speed_slope(const ff* r, ff v, float& q)
+    {
+        if constexpr (CODE == 0) {
+            float sn, cs;
+            sincospif(fmaf(v.hi, (float)ELLIPSE_PIECE_SCALE, r[2].hi), &sn, &cs);
+            q = (float)(PI * ELLIPSE_PIECE_SCALE) * r[0].hi * sn * cs;
+            return speed(r, v);
+        } else {
+            ff s{0.0f, 0.0f};
+            float t = 0.0f;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                ff acc = r[(P - 1) * D + d];
+                float dacc = 0.0f;
+#pragma unroll
+                for (int k = P - 2; k >= 0; --k) {
+                    dacc = fmaf(dacc, v.hi, acc.hi);
+                    acc = ff_fma(acc, v, r[k * D + d]);
+                }
+                s = d == 0 ? ff_mul(acc, acc) : ff_fma(acc, acc, s);
+                t = fmaf(acc.hi, dacc, t);
+            }
+            q = t;
+            return ff_sqrt(s);
+        }
+    }
+};
+
+// float-float panel: K15, G7, right-end speed and slope of [vlo, vlo + 2 hw]
+// with vlo = -1 + k 2^(1-depth) built exactly from the integer k.
+template <int CODE>
+__device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, int depth, ff& K, ff& G, ff& fend,
+                                             float& qend)
+{
+    const float hw = __int_as_float((127 - depth) << 23);  // 2^-depth, exact
+    const float kh = (float)(unsigned)(k >> 24), kl = (float)(unsigned)(k & 0xFFFFFFull);
+    const float sh = __int_as_float((127 + 25 - depth) << 23), sl = 2.0f * hw;  // 2^(25-depth), 2^(1-depth)
+    const ff vlo = ff_add_f(two_sum(-1.0f, kh * sh), kl * sl);
+    const ff mid = ff_add_f(vlo, hw);
+    const ff fc = EvalFF<CODE>::speed(r, mid);
+    ff kk = ff_mul(to_ff(split_const(gk_wk(7))), fc);
+    ff gg = ff_mul(to_ff(split_const(gk_wg(7))), fc);
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+        const ff dx = ff_scale(to_ff(split_const(gk_x(i))), hw);
+        const ff s = ff_add(EvalFF<CODE>::speed(r, ff_add(mid, ff_neg(dx))), EvalFF<CODE>::speed(r, ff_add(mid, dx)));
+        kk = ff_fma(to_ff(split_const(gk_wk(i))), s, kk);
+        if (i & 1) gg = ff_fma(to_ff(split_const(gk_wg(i))), s, gg);
+    }
+    fend = EvalFF<CODE>::speed_slope(r, ff_add_f(vlo, 2.0f * hw), qend);
+    K = ff_scale(kk, hw);
+    G = ff_scale(gg, hw);
+}
+
+__device__ __forceinline__ void load_ff_dyn(int code, const float2* __restrict__ seg, ff* r)
+{
+    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: EvalFF<C>::load(seg, r); break;
+        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+    default: break;
+    }
+}
+
+__device__ __forceinline__ void panel_ff_dyn(int code, const ff* r, unsigned long long k, int depth, ff& K, ff& G,
+                                             ff& fend, float& qend)
+{
+    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: panel_k15_ff<C>(r, k, depth, K, G, fend, qend); break;
+        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+    default: K = G = fend = ff{0.0f, 0.0f}; qend = 0.0f; break;
+    }
+}
+
+template <int CODE>
+__device__ __forceinline__ ff speed_ff_of(int code, const ff* r, ff v)
+{
+    if constexpr (CODE >= 0) {
+        return EvalFF<CODE>::speed(r, v);
+    } else {
+        switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: return EvalFF<C>::speed(r, v);
+            GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+        default: return ff{0.0f, 0.0f};
+        }
+    }
+}
+
+template <int CODE>
+__device__ __forceinline__ ff speed_slope_ff_of(int code, const ff* r, ff v, float& q)
+{
+    if constexpr (CODE >= 0) {
+        return EvalFF<CODE>::speed_slope(r, v, q);
+    } else {
+        switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: return EvalFF<C>::speed_slope(r, v, q);
+            GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+        default: q = 0.0f; return ff{0.0f, 0.0f};
+        }
+    }
+}
+
+}  // namespace gcv

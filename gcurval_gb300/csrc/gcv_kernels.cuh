@@ -3,76 +3,9 @@
 // instantiates them, and by the header-only plugin path.
 #pragma once
 
-#include "gcv_device.cuh"
+#include "gcv_table.cuh"
 
 namespace gcv {
-
-// ----------------------------------------------------------- device views
-struct Batch {
-    int64_t n_curve;
-    int64_t n_seg;
-    const uint8_t* kind;
-    const uint8_t* degree;
-    const uint8_t* dim;
-    const int64_t* knot_off;
-    const double* knots;
-    const int64_t* ctrl_off;
-    const double* ctrl;
-    const int64_t* seg_off;   // [n_curve + 1] first segment of each curve
-    const int64_t* coef_off;  // [n_curve + 1] first coefficient (double) of each curve
-    const int* seg_curve;     // [n_seg] curve of each segment
-};
-
-// counters in one device array (reset before each phase that uses them)
-enum Counter {
-    C_WORK = 0,       // length work-queue head
-    C_LEAF_TOP = 1,   // leaf-pool bump pointer
-    C_DEEP = 2,       // number of segments on the deep list
-    C_PANELS = 3,
-    C_CAPPED = 4,
-    C_NEWTON = 5,
-    C_ERR = 6,        // error bits (ERR_*)
-    C_NONFINITE = 7,
-    C_SCAN_TILE = 8,  // scan tile ticket
-    C_COUNT = 16
-};
-enum ErrBits { ERR_POOL = 1, ERR_SCAN_TIMEOUT = 2, ERR_BAD_KNOTS = 4, ERR_DEEP_LIST = 8 };
-
-struct Table {
-    double* coef;      // per-segment evaluation data (code_stride doubles), FP64 path
-    float2* coef_ff;   // the same as float-float pairs (mixed path; NULL otherwise)
-    double* seg_t0;    // curve parameter at v = -1
-    double* seg_t1;    // curve parameter at v = +1
-    double* seg_f0;    // f(-1)
-    double* seg_q0;    // (f f')(-1)
-    double* seg_len;   // length of each segment
-    double* seg_cum;   // cumulative length at the end of each segment (within its curve)
-    double* curve_len;
-    int64_t* leaf_off;
-    int* leaf_cnt;
-    double* leaf_v;    // right end (local v) of each leaf panel
-    double* leaf_cum;  // cumulative length within the segment at that end
-    double* leaf_f;    // f at that end
-    double* leaf_q;    // f * df/dv at that end
-    int64_t leaf_cap;
-    int* deep_list;
-    int64_t deep_cap;
-    unsigned long long* ctr;
-    int* scan_status;  // per scan tile: 0 none, 1 aggregate, 2 inclusive
-    int* scan_flag;
-    double* scan_hi;
-    double* scan_lo;
-};
-
-__device__ __forceinline__ int curve_code(const Batch& b, int64_t c)
-{
-    return b.kind[c] == 0 ? CODE_ELLIPSE : bs_code(b.degree[c], b.dim[c]);
-}
-
-__device__ __forceinline__ void raise_err(const Table& t, unsigned bits)
-{
-    atomicOr(t.ctr + C_ERR, (unsigned long long)bits);
-}
 
 // ---------------------------------------------------------------- set-up
 // One thread per segment: segment -> curve map consumer; writes the
@@ -127,16 +60,20 @@ __device__ void setup_bspline_seg(const Batch& b, const Table& t, int64_t s, int
 
 __device__ inline void setup_ellipse_seg(const Batch& b, const Table& t, int64_t s, int64_t c)
 {
+    const int j = int(s - b.seg_off[c]);  // piece 0 .. ELLIPSE_PIECES - 1
     const double* e = b.ctrl + b.ctrl_off[c];
     const double a = e[0], bb = e[1];
     double sr, cr;
     sincos(e[2], &sr, &cr);
-    const double out[8] = {a * a - bb * bb, bb * bb, a, bb, cr, sr, e[3], e[4]};
-    store_coef<8>(t, b.coef_off[c], out);
-    t.seg_t0[s] = 0.0;
-    t.seg_t1[s] = 2.0 * PI;
-    t.seg_f0[s] = PI * fabs(bb);
-    t.seg_q0[s] = 0.0;  // sin(pi v) = 0 at v = -1
+    constexpr double h = PI * ELLIPSE_PIECE_SCALE;
+    const double w0 = (2 * j + 1) * ELLIPSE_PIECE_SCALE - 1.0;
+    const double out[9] = {(a * a - bb * bb) * (h * h), bb * bb * (h * h), w0, a, bb, cr, sr, e[3], e[4]};
+    store_coef<9>(t, b.coef_off[c] + (int64_t)j * 9, out);
+    t.seg_t0[s] = (2.0 * PI * ELLIPSE_PIECE_SCALE) * j;
+    t.seg_t1[s] = j + 1 == ELLIPSE_PIECES ? 2.0 * PI : (2.0 * PI * ELLIPSE_PIECE_SCALE) * (j + 1);
+    double q0;
+    t.seg_f0[s] = ellipse_speed_slope(out[0], out[1], w0, -1.0, q0);
+    t.seg_q0[s] = q0;
 }
 
 static __global__ void k_setup(Batch b, Table t)
@@ -164,6 +101,27 @@ static __global__ void k_seg_curve(Batch b, int* seg_curve)
          c += (int64_t)gridDim.x * blockDim.x) {
         for (int64_t s = b.seg_off[c]; s < b.seg_off[c + 1]; ++s) seg_curve[s] = int(c);
     }
+}
+
+// grouped segment list: the segments of curve c go to dst[c], dst[c] + 1, ...
+static __global__ void k_group_segments(Batch b, const int64_t* __restrict__ dst, int* __restrict__ list)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < b.n_seg;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int c = b.seg_curve[s];
+        list[dst[c] + (s - b.seg_off[c])] = int(s);
+    }
+}
+
+// sum of leaf_cnt over a list of segments (one atomic per warp)
+static __global__ void k_deep_total(const int* __restrict__ list, int64_t n, const int* __restrict__ leaf_cnt,
+                                    unsigned long long* __restrict__ out)
+{
+    unsigned long long acc = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        acc += (unsigned long long)leaf_cnt[list[i]];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
 }
 
 // ------------------------------------------------- compensated scan

@@ -1,0 +1,7 @@
+// Length-pass instantiations: planar B-splines of degree 4 and 5.
+#include "gcv_length_impl.cuh"
+
+namespace gcv {
+GCV_LENGTH_INST2(0, bs_code(4, 2))
+GCV_LENGTH_INST2(0, bs_code(5, 2))
+}  // namespace gcv

@@ -1,0 +1,10 @@
+// Length-pass instantiations: spatial B-splines of degree 1 to 3.
+#include "gcv_length_impl.cuh"
+
+namespace gcv {
+GCV_LENGTH_INST2(0, bs_code(1, 3))
+GCV_LENGTH_INST2(0, bs_code(2, 3))
+GCV_LENGTH_INST2(0, bs_code(3, 3))
+GCV_LENGTH_INST2(1, bs_code(3, 3))
+GCV_LENGTH_INST2(2, bs_code(3, 3))
+}  // namespace gcv

@@ -1,0 +1,10 @@
+// Length-pass instantiations: ellipses, and the runtime-dispatch deep passes.
+#include "gcv_length_impl.cuh"
+
+namespace gcv {
+GCV_LENGTH_INST2(0, CODE_ELLIPSE)
+GCV_LENGTH_INST2(1, CODE_ELLIPSE)
+GCV_LENGTH_INST2(2, CODE_ELLIPSE)
+GCV_LENGTH_INST2(1, -1)
+GCV_LENGTH_INST2(2, -1)
+}  // namespace gcv

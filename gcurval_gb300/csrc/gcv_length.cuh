@@ -23,8 +23,8 @@
 // gcurval/detail/cuda/arclength_calculate.h:259-323).
 #pragma once
 
-#include "gcv_kernels.cuh"
-#include "gcv_mixed.cuh"
+#include "gcv_table.cuh"
+#include "gcv_ff.cuh"
 
 namespace gcv {
 
@@ -39,266 +39,19 @@ struct LengthParams {
     double rtol;
     int max_depth;
     int collect;
-    const int* list;  // segments to process (deep passes); NULL: all segments
+    const int* list;  // segments to process; NULL: segments 0 .. n_items - 1
     int64_t n_items;
     const float2* coef_ff;  // float-float copy of the coefficients (PREC 1)
+    unsigned long long* work;  // work-queue head of this launch (starts at 0)
 };
 
-// K15, G7 and the right-end speed of panel [vlo, vlo + 2 hw].
-template <int CODE>
-__device__ __forceinline__ void panel_k15(const double* r, double vlo, double hw, double& K, double& G,
-                                          double& fend, double& qend)
-{
-    const double mid = vlo + hw;
-    const double fc = Eval<CODE>::speed(r, mid);
-    double k = gk_wk(7) * fc;
-    double g = gk_wg(7) * fc;
-#pragma unroll
-    for (int i = 0; i < 7; ++i) {
-        const double dx = hw * gk_x(i);
-        const double s = Eval<CODE>::speed(r, mid - dx) + Eval<CODE>::speed(r, mid + dx);
-        k = fma(gk_wk(i), s, k);
-        if (i & 1) g = fma(gk_wg(i), s, g);
-    }
-    fend = Eval<CODE>::speed_slope(r, vlo + 2.0 * hw, qend);
-    K = k * hw;
-    G = g * hw;
-}
-
-__device__ __forceinline__ void panel_dyn(int code, const double* r, double vlo, double hw, double& K, double& G,
-                                          double& fend, double& qend)
-{
-    switch (code) {
-#define GCV_CASE(C)                                                                                \
-    case C: panel_k15<C>(r, vlo, hw, K, G, fend, qend); break;
-        GCV_FOR_EACH_CODE(GCV_CASE)
-#undef GCV_CASE
-    default: K = G = fend = qend = 0.0; break;
-    }
-}
-
-__device__ __forceinline__ int warp_incl_scan(int x, int lane)
-{
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, x, d);
-        if (lane >= d) x += y;
-    }
-    return x;
-}
-
-// PREC 0: FP64 panels; PREC 1: float-float panels (GCV_MIXED), whose K15 /
-// G7 / end values enter the same FP64 bookkeeping (error test, leaf table).
-template <int MODE, int CODE, int PREC = 0>
-__global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
-{
-    __shared__ double lf_v[MODE == 0 ? LCAP : 1][LK_THREADS];
-    __shared__ double lf_c[MODE == 0 ? LCAP : 1][LK_THREADS];
-    __shared__ double lf_f[MODE == 0 ? LCAP : 1][LK_THREADS];
-    __shared__ double lf_q[MODE == 0 ? LCAP : 1][LK_THREADS];
-
-    const Batch& b = P.b;
-    const Table& t = P.t;
-    const int lane = threadIdx.x & 31;
-    const int tid = threadIdx.x;
-    const unsigned FULL = 0xffffffffu;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    // round-off floor of the error test: 50 units of the working precision
-    // (FP64: 2^-52; float-float: ~2^-46)
-    const double eps50 = PREC == 1 ? 50.0 * 1.4210854715202004e-14 : 50.0 * 2.220446049250313e-16;
-
-    bool active = false, exhausted = false;
-    int64_t s = 0, pool = 0;
-    int code = CODE >= 0 ? CODE : 0;
-    double r[PREC == 0 ? MAX_COEF : 1];
-    ff rf[PREC == 1 ? MAX_COEF : 1];
-    unsigned long long k = 0;
-    int depth = 0, nleaf = 0;
-    double cum = 0.0, tol_unit = 0.0;
-    long long panels = 0;
-    unsigned long long my_panels = 0, my_capped = 0, my_nonfinite = 0;
-
-    for (;;) {
-        bool fin = false, ovf = false;
-        // ---- refill idle lanes with one atomic per warp
-        const bool need = !active && !exhausted;
-        const unsigned m = __ballot_sync(FULL, need);
-        if (m) {
-            const int leader = __ffs(m) - 1;
-            unsigned long long base = 0;
-            if (lane == leader) base = atomicAdd(t.ctr + C_WORK, (unsigned long long)__popc(m));
-            base = __shfl_sync(FULL, base, leader);
-            if (need) {
-                const int64_t item = (int64_t)base + __popc(m & lt_mask);
-                if (item >= P.n_items) {
-                    exhausted = true;
-                } else {
-                    s = P.list ? (int64_t)P.list[item] : item;
-                    const int64_t c = b.seg_curve[s];
-                    if (CODE < 0) code = curve_code(b, c);
-                    const int64_t ci = b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
-                    if constexpr (PREC == 1) {
-                        if constexpr (CODE >= 0)
-                            EvalFF<(CODE >= 0 ? CODE : 0)>::load(P.coef_ff + ci, rf);
-                        else
-                            load_ff_dyn(code, P.coef_ff + ci, rf);
-                    } else {
-                        if constexpr (CODE >= 0)
-                            Eval<(CODE >= 0 ? CODE : 0)>::load_speed(t.coef + ci, r);
-                        else
-                            load_speed_dyn(code, t.coef + ci, r);
-                    }
-                    k = 0;
-                    depth = 0;
-                    nleaf = 0;
-                    cum = 0.0;
-                    panels = 0;
-                    if (MODE == 2) {
-                        pool = (int64_t)atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)t.leaf_cnt[s]);
-                        if (pool + t.leaf_cnt[s] > t.leaf_cap) {
-                            raise_err(t, ERR_POOL);
-                            pool = -1;
-                        }
-                    }
-                    if (t.seg_t1[s] == t.seg_t0[s]) {  // zero-width knot interval: one empty leaf
-                        if (MODE == 0) {
-                            lf_v[0][tid] = 1.0;
-                            lf_c[0][tid] = 0.0;
-                            lf_f[0][tid] = 0.0;
-                            lf_q[0][tid] = 0.0;
-                        } else if (MODE == 2 && pool >= 0) {
-                            t.leaf_v[pool] = 1.0;
-                            t.leaf_cum[pool] = 0.0;
-                            t.leaf_f[pool] = 0.0;
-                            t.leaf_q[pool] = 0.0;
-                        }
-                        nleaf = 1;
-                        fin = true;
-                    } else if (MODE != 2 || pool >= 0) {
-                        active = true;
-                    }
-                }
-            }
-        }
-        // ---- one panel per active lane
-        if (active) {
-            const double hw = pow2_neg(depth);
-            const double vlo = fma(__ull2double_rn(k), 2.0 * hw, -1.0);
-            double K, G, fend, qend;
-            if constexpr (PREC == 1) {
-                ff Kf, Gf, ff_end;
-                float q32;
-                if constexpr (CODE >= 0)
-                    panel_k15_ff<(CODE >= 0 ? CODE : 0)>(rf, k, depth, Kf, Gf, ff_end, q32);
-                else
-                    panel_ff_dyn(code, rf, k, depth, Kf, Gf, ff_end, q32);
-                K = ff_to_double(Kf);
-                G = ff_to_double(Gf);
-                fend = ff_to_double(ff_end);
-                qend = (double)q32;
-            } else {
-                if constexpr (CODE >= 0)
-                    panel_k15<(CODE >= 0 ? CODE : 0)>(r, vlo, hw, K, G, fend, qend);
-                else
-                    panel_dyn(code, r, vlo, hw, K, G, fend, qend);
-            }
-            if (depth == 0) tol_unit = P.rtol * fabs(K);
-            ++panels;
-            const double err = fabs(K - G);
-            const bool finite = isfinite(K) && isfinite(G);
-            const bool at_cap = depth >= P.max_depth || panels >= PANEL_BUDGET;
-            const bool ok = err <= fmax(tol_unit * hw, eps50 * fabs(K));
-            if (ok || at_cap || !finite) {
-                if (!ok && finite) ++my_capped;
-                if (!finite) ++my_nonfinite;
-                cum += K;
-                const double vr = vlo + 2.0 * hw;
-                if (MODE == 0) {
-                    if (nleaf < LCAP) {
-                        lf_v[nleaf][tid] = vr;
-                        lf_c[nleaf][tid] = cum;
-                        lf_f[nleaf][tid] = fend;
-                        lf_q[nleaf][tid] = qend;
-                    } else {
-                        ovf = true;
-                    }
-                } else if (MODE == 2) {
-                    t.leaf_v[pool + nleaf] = vr;
-                    t.leaf_cum[pool + nleaf] = cum;
-                    t.leaf_f[pool + nleaf] = fend;
-                    t.leaf_q[pool + nleaf] = qend;
-                }
-                ++nleaf;
-                ++k;
-                const int tz = __ffsll((long long)k) - 1;
-                k >>= tz;
-                depth -= tz;
-                if (ovf) {
-                    active = false;
-                } else if (depth == 0) {
-                    active = false;
-                    fin = true;
-                }
-            } else {
-                k <<= 1;
-                ++depth;
-            }
-            if (!active) my_panels += (unsigned long long)panels;
-        }
-        // ---- finished segments: outputs (leaf-pool offsets reserved per warp)
-        if (MODE == 0) {
-            const unsigned fm = __ballot_sync(FULL, fin);
-            if (fm) {
-                const int x = fin ? nleaf : 0;
-                const int incl = warp_incl_scan(x, lane);
-                const int total = __shfl_sync(FULL, incl, 31);
-                unsigned long long base = 0;
-                if (lane == 0) base = atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)total);
-                base = __shfl_sync(FULL, base, 0);
-                if (fin) {
-                    const int64_t off = (int64_t)base + incl - x;
-                    if (off + nleaf <= t.leaf_cap) {
-                        for (int i = 0; i < nleaf; ++i) {
-                            t.leaf_v[off + i] = lf_v[i][tid];
-                            t.leaf_cum[off + i] = lf_c[i][tid];
-                            t.leaf_f[off + i] = lf_f[i][tid];
-                            t.leaf_q[off + i] = lf_q[i][tid];
-                        }
-                    } else {
-                        raise_err(t, ERR_POOL);
-                    }
-                    t.seg_len[s] = nleaf == 1 && t.seg_t1[s] == t.seg_t0[s] ? 0.0 : cum;
-                    t.leaf_off[s] = off;
-                    t.leaf_cnt[s] = nleaf;
-                }
-            }
-            if (ovf) {
-                const unsigned long long o = atomicAdd(t.ctr + C_DEEP, 1ull);
-                if ((int64_t)o < t.deep_cap)
-                    t.deep_list[o] = int(s);
-                else
-                    raise_err(t, ERR_DEEP_LIST);
-            }
-        } else if (fin) {
-            if (MODE == 1) t.leaf_cnt[s] = nleaf;
-            if (MODE == 2) {
-                t.seg_len[s] = t.seg_t1[s] == t.seg_t0[s] ? 0.0 : cum;
-                t.leaf_off[s] = pool;
-            }
-        }
-        if (__all_sync(FULL, exhausted && !active)) break;
-    }
-    // ---- statistics
-    for (int o = 16; o > 0; o >>= 1) {
-        my_panels += __shfl_xor_sync(FULL, my_panels, o);
-        my_capped += __shfl_xor_sync(FULL, my_capped, o);
-        my_nonfinite += __shfl_xor_sync(FULL, my_nonfinite, o);
-    }
-    if (lane == 0) {
-        if (P.collect && my_panels) atomicAdd(t.ctr + C_PANELS, my_panels);
-        if (my_capped) atomicAdd(t.ctr + C_CAPPED, my_capped);
-        if (my_nonfinite) atomicAdd(t.ctr + C_NONFINITE, my_nonfinite);
-    }
-}
+// Launches k_length<MODE, CODE, PREC> over P (persistent grid sized from the
+// occupancy and sm_count); defined with the kernel in gcv_length_impl.cuh and
+// instantiated per curve code in the gcv_len_*.cu units.
+//   MODE 0: main pass; MODE 1: count pass of the deep list; MODE 2: write pass.
+//   CODE: curve code, or -1 for runtime dispatch per segment.
+//   PREC 0: FP64 panels; 1: float-float panels.
+template <int MODE, int CODE, int PREC>
+cudaError_t length_launch(const LengthParams& P, cudaStream_t stream, int sm_count);
 
 }  // namespace gcv

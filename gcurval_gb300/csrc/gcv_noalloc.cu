@@ -30,7 +30,8 @@
 #include <mutex>
 #include <string>
 
-#include "gcv_length.cuh"
+#include "gcv_kernels.cuh"
+#include "gcv_length_impl.cuh"
 
 extern "C" gcv_status gcv_internal_fail(gcv_status s, const char* msg);
 
