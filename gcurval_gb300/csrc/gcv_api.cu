@@ -13,9 +13,9 @@
 #include <string>
 #include <vector>
 
-#include "gcv_kernels.cuh"
 #include "gcv_length.cuh"
-#include "gcv_mixed.cuh"
+#include "gcv_sample.cuh"
+#include "gcv_table_kernels.cuh"
 
 using namespace gcv;
 
@@ -132,9 +132,12 @@ struct gcv_ctx {
     std::vector<int64_t> h_seg_off;
     std::vector<uint8_t> h_kind, h_degree;
     std::vector<double> h_start;  // first parameter value of each curve
-    // batches that mix curve codes: segments grouped by code, one range per code
-    DBuf<int> seg_list;
-    std::vector<CodeRange> code_ranges;
+    // batches that mix curve codes: segments and curves grouped by code, one
+    // range per code in each list
+    DBuf<int> seg_list, curve_list;
+    std::vector<CodeRange> code_ranges, curve_ranges;
+    std::vector<int> h_curve_list;
+    DBuf<int64_t> list_sample_off;  // sample-count prefix in curve_list order
 
     // table
     DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_q0, seg_len, seg_cum, curve_len;
@@ -237,6 +240,8 @@ void destroy_ctx(gcv_ctx* c)
     c->coef_off.release();
     c->seg_curve.release();
     c->seg_list.release();
+    c->curve_list.release();
+    c->list_sample_off.release();
     c->coef.release();
     c->seg_t0.release();
     c->seg_t1.release();
@@ -377,6 +382,21 @@ gcv_status finish_create(gcv_ctx* c, const uint8_t* kind, const uint8_t* degree,
             dst[(size_t)i] = nb;
             nb += seg_off[(size_t)i + 1] - seg_off[(size_t)i];
         }
+        // curves grouped the same way (sampling launches)
+        std::vector<int64_t> curve_base(64, 0), per_code_curves(64, 0);
+        for (int64_t i = 0; i < n; ++i) per_code_curves[(size_t)code_of[(size_t)i]]++;
+        c->curve_ranges.clear();
+        int64_t cat = 0;
+        for (int cd = 0; cd < 64; ++cd) {
+            curve_base[(size_t)cd] = cat;
+            if (per_code_curves[(size_t)cd] > 0) {
+                c->curve_ranges.push_back(CodeRange{cd, cat, cat + per_code_curves[(size_t)cd]});
+                cat += per_code_curves[(size_t)cd];
+            }
+        }
+        c->h_curve_list.assign((size_t)n, 0);
+        for (int64_t i = 0; i < n; ++i) c->h_curve_list[(size_t)(curve_base[(size_t)code_of[(size_t)i]]++)] = (int)i;
+        CHECK(upload(c->curve_list, c->h_curve_list.data(), (size_t)n, c->stream));
         DBuf<int64_t> d_dst;
         struct Release {
             DBuf<int64_t>& b;
@@ -550,6 +570,26 @@ gcv_status launch_main_pass(gcv_ctx* c, LengthParams P)
     return GCV_OK;
 }
 
+gcv_status launch_setup_list(gcv_ctx* c, const CodeRange& r)
+{
+    const int64_t n = r.end - r.begin;
+    if (n <= 0) return GCV_OK;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 64));
+    const Batch b = batch_view(c);
+    const Table t = table_view(c);
+    const int* list = c->seg_list.p + r.begin;
+    switch (r.code) {
+#define GCV_CASE(C)                                                                                \
+    case C: k_setup_list<C><<<blocks, 256, 0, c->stream>>>(b, t, list, n); break;
+        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+    default: return fail(GCV_ERR_INVALID, "no set-up kernel for curve code " + std::to_string(r.code));
+    }
+    CU(cudaGetLastError());
+    c->stats.n_launches++;
+    return GCV_OK;
+}
+
 gcv_status build_table(gcv_ctx* c)
 {
     CHECK(ensure_table_buffers(c));
@@ -558,10 +598,12 @@ gcv_status build_table(gcv_ctx* c)
     const int setup_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 64));
     CU(cudaEventRecord(c->ev[0], c->stream));
     CU(cudaMemsetAsync(c->ctr.p, 0, C_COUNT * sizeof(unsigned long long), c->stream));
-    if (c->n_seg > 0) {
+    if (c->n_seg > 0 && c->code >= 0) {
         k_setup<<<setup_blocks, 256, 0, c->stream>>>(b, table_view(c));
         CU(cudaGetLastError());
         c->stats.n_launches++;
+    } else if (c->n_seg > 0) {
+        for (const CodeRange& r : c->code_ranges) CHECK(launch_setup_list(c, r));
     }
     CU(cudaEventRecord(c->ev[1], c->stream));
     for (int attempt = 0;; ++attempt) {
@@ -651,6 +693,25 @@ gcv_status build_table(gcv_ctx* c)
 
 // ---------------------------------------------------------------- sampling
 
+gcv_status launch_sampler(gcv_ctx* c, int code, const SampleParams& P, int64_t n)
+{
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + SAMPLE_THREADS - 1) / SAMPLE_THREADS,
+                                                               (int64_t)sm_count() * 64));
+    const bool mixed = c->opt.precision == GCV_MIXED;
+    const float2* cf = c->coef_ff.p;
+    cudaError_t e = cudaErrorInvalidValue;
+    switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: e = mixed ? sample_launch<C, 1>(P, cf, c->stream, grid) : sample_launch<C, 0>(P, cf, c->stream, grid); break;
+        GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+    default: return fail(GCV_ERR_INVALID, "no sampling kernel for curve code " + std::to_string(code));
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "sampling kernel launch");
+    c->stats.n_launches++;
+    return GCV_OK;
+}
+
 gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, const double* d_pos, int64_t total, int is_relative,
                         int what, double* d_out)
 {
@@ -670,26 +731,30 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, const double* d
         P.n_samples = total;
         P.collect = c->opt.collect_stats;
         P.rtol = c->opt.rtol;
-        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((total + SAMPLE_THREADS - 1) / SAMPLE_THREADS,
-                                                                   (int64_t)sm_count() * 64));
-        if (c->opt.precision == GCV_MIXED) {
-            const float2* cf = c->coef_ff.p;
-            switch (c->code) {
-            case CODE_ELLIPSE: k_sample_ff<CODE_ELLIPSE><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P, cf); break;
-            case bs_code(3, 2): k_sample_ff<bs_code(3, 2)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P, cf); break;
-            case bs_code(3, 3): k_sample_ff<bs_code(3, 3)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P, cf); break;
-            default: k_sample_ff<-1><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P, cf); break;
-            }
+        P.curve_list = nullptr;
+        P.list_off = nullptr;
+        P.cb = P.ce = 0;
+        if (c->code >= 0) {
+            CHECK(launch_sampler(c, c->code, P, total));
         } else {
-            switch (c->code) {
-            case CODE_ELLIPSE: k_sample<CODE_ELLIPSE><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
-            case bs_code(3, 2): k_sample<bs_code(3, 2)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
-            case bs_code(3, 3): k_sample<bs_code(3, 3)><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
-            default: k_sample<-1><<<grid, SAMPLE_THREADS, 0, c->stream>>>(P); break;
+            // one launch per curve code over the grouped curve list
+            const int64_t n = c->n_curve;
+            std::vector<int64_t> lo((size_t)n + 1, 0);
+            for (int64_t j = 0; j < n; ++j) {
+                const int cj = c->h_curve_list[(size_t)j];
+                lo[(size_t)j + 1] = lo[(size_t)j] + (c->h_sample_off[(size_t)cj + 1] - c->h_sample_off[(size_t)cj]);
+            }
+            CHECK(upload(c->list_sample_off, lo.data(), lo.size(), c->stream));
+            P.curve_list = c->curve_list.p;
+            P.list_off = c->list_sample_off.p;
+            for (const CodeRange& r : c->curve_ranges) {
+                const int64_t ns = lo[(size_t)r.end] - lo[(size_t)r.begin];
+                if (ns == 0) continue;
+                P.cb = r.begin;
+                P.ce = r.end;
+                CHECK(launch_sampler(c, r.code, P, ns));
             }
         }
-        CU(cudaGetLastError());
-        c->stats.n_launches++;
     }
     CU(cudaEventRecord(c->ev[5], c->stream));
     c->ev_sample = true;

@@ -1,0 +1,10 @@
+// Length-pass and sampling instantiations: spatial B-splines of degree 4 and 5.
+#include "gcv_length_impl.cuh"
+#include "gcv_sample_impl.cuh"
+
+namespace gcv {
+GCV_LENGTH_INST2(0, bs_code(4, 3))
+GCV_LENGTH_INST2(0, bs_code(5, 3))
+GCV_SAMPLE_INST2(bs_code(4, 3))
+GCV_SAMPLE_INST2(bs_code(5, 3))
+}  // namespace gcv

@@ -318,11 +318,13 @@ __device__ void bspline_setup(const double* __restrict__ kv, const double* __res
 #pragma unroll
         for (int k = 0; k <= P; ++k) N[r][k] = 0.0;
     N[0][0] = 1.0;
+    // at step j the basis polynomials N[0..j-1] have degree j - 1 and the
+    // new ones degree j: the loops run over those coefficients only
 #pragma unroll
     for (int j = 1; j <= P; ++j) {
         double saved[P + 1];
 #pragma unroll
-        for (int k = 0; k <= P; ++k) saved[k] = 0.0;
+        for (int k = 0; k <= j; ++k) saved[k] = 0.0;
 #pragma unroll
         for (int r = 0; r < j; ++r) {
             const double kr = kv[span + r + 1];      // right[r+1] = kr - u
@@ -330,17 +332,24 @@ __device__ void bspline_setup(const double* __restrict__ kv, const double* __res
             const double inv = 1.0 / (kr - kl);
             double temp[P + 1];
 #pragma unroll
-            for (int k = 0; k <= P; ++k) temp[k] = N[r][k] * inv;
+            for (int k = 0; k < j; ++k) temp[k] = N[r][k] * inv;
             const double ra = kr - m, la = m - kl;  // right = ra - w v, left = la + w v
 #pragma unroll
-            for (int k = P; k >= 0; --k) {
-                const double tk = temp[k], tk1 = k > 0 ? temp[k - 1] : 0.0;
-                N[r][k] = saved[k] + (ra * tk - w * tk1);
-                saved[k] = la * tk + w * tk1;
+            for (int k = j; k >= 0; --k) {
+                if (k == j) {  // only the v * temp[j-1] terms reach degree j
+                    N[r][k] = saved[k] - w * temp[k - 1];
+                    saved[k] = w * temp[k - 1];
+                } else if (k == 0) {
+                    N[r][k] = saved[k] + ra * temp[k];
+                    saved[k] = la * temp[k];
+                } else {
+                    N[r][k] = saved[k] + (ra * temp[k] - w * temp[k - 1]);
+                    saved[k] = la * temp[k] + w * temp[k - 1];
+                }
             }
         }
 #pragma unroll
-        for (int k = 0; k <= P; ++k) N[j][k] = saved[k];
+        for (int k = 0; k <= j; ++k) N[j][k] = saved[k];
     }
     // position: C(v) = sum_i P_{span-P+i} N_i(v).  The basis sums to one, so
     // combining differences P_i - P_0 and adding P_0 back to the constant

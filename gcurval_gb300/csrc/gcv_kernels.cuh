@@ -76,209 +76,6 @@ __device__ inline void setup_ellipse_seg(const Batch& b, const Table& t, int64_t
     t.seg_q0[s] = q0;
 }
 
-static __global__ void k_setup(Batch b, Table t)
-{
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < b.n_seg;
-         s += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = b.seg_curve[s];
-        switch (curve_code(b, c)) {
-        case CODE_ELLIPSE: setup_ellipse_seg(b, t, s, c); break;
-#define GCV_SETUP_CASE(P, D)                                                                       \
-    case bs_code(P, D): setup_bspline_seg<P, D>(b, t, s, c); break;
-            GCV_SETUP_CASE(1, 2) GCV_SETUP_CASE(2, 2) GCV_SETUP_CASE(3, 2) GCV_SETUP_CASE(4, 2)
-            GCV_SETUP_CASE(5, 2) GCV_SETUP_CASE(1, 3) GCV_SETUP_CASE(2, 3) GCV_SETUP_CASE(3, 3)
-            GCV_SETUP_CASE(4, 3) GCV_SETUP_CASE(5, 3)
-#undef GCV_SETUP_CASE
-        default: break;
-        }
-    }
-}
-
-// segment -> curve map (thread per curve writes its range)
-static __global__ void k_seg_curve(Batch b, int* seg_curve)
-{
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < b.n_curve;
-         c += (int64_t)gridDim.x * blockDim.x) {
-        for (int64_t s = b.seg_off[c]; s < b.seg_off[c + 1]; ++s) seg_curve[s] = int(c);
-    }
-}
-
-// grouped segment list: the segments of curve c go to dst[c], dst[c] + 1, ...
-static __global__ void k_group_segments(Batch b, const int64_t* __restrict__ dst, int* __restrict__ list)
-{
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < b.n_seg;
-         s += (int64_t)gridDim.x * blockDim.x) {
-        const int c = b.seg_curve[s];
-        list[dst[c] + (s - b.seg_off[c])] = int(s);
-    }
-}
-
-// sum of leaf_cnt over a list of segments (one atomic per warp)
-static __global__ void k_deep_total(const int* __restrict__ list, int64_t n, const int* __restrict__ leaf_cnt,
-                                    unsigned long long* __restrict__ out)
-{
-    unsigned long long acc = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        acc += (unsigned long long)leaf_cnt[list[i]];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
-}
-
-// ------------------------------------------------- compensated scan
-// Single-pass segmented inclusive scan of segment lengths (segments of one
-// curve are contiguous; a curve's first segment starts a new sum) with
-// decoupled look-back between tiles and double-double (two-sum) arithmetic,
-// replacing the reference's per-segment Brent-Kung scan plus one thread per
-// curve doing a sequential Kahan sum (gcurval/detail/cuda/kernel/generic.inl.cuh:52-137).
-constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 4;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-constexpr long long SCAN_SPIN_LIMIT = 1ll << 22;
-
-struct DD {
-    double hi, lo;
-};
-__device__ __forceinline__ DD dd_add(DD a, DD b)
-{
-    const double s = a.hi + b.hi;
-    const double bb = s - a.hi;
-    double e = (a.hi - (s - bb)) + (b.hi - bb);
-    e += a.lo + b.lo;
-    const double h = s + e;
-    return DD{h, e - (h - s)};
-}
-struct SegVal {
-    int flag;  // a curve starts inside this range
-    DD v;      // sum since the last start
-};
-// a earlier, b later
-__device__ __forceinline__ SegVal seg_combine(const SegVal& a, const SegVal& b)
-{
-    if (b.flag) return b;
-    return SegVal{a.flag, dd_add(a.v, b.v)};
-}
-__device__ __forceinline__ SegVal shfl_up_sv(const SegVal& x, int d)
-{
-    SegVal y;
-    y.flag = __shfl_up_sync(0xffffffffu, x.flag, d);
-    y.v.hi = __shfl_up_sync(0xffffffffu, x.v.hi, d);
-    y.v.lo = __shfl_up_sync(0xffffffffu, x.v.lo, d);
-    return y;
-}
-
-static __global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, int64_t n_tiles)
-{
-    __shared__ int s_tile;
-    __shared__ SegVal s_warp[SCAN_THREADS / 32];
-    __shared__ SegVal s_prefix;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(t.ctr + C_SCAN_TILE, 1ull);
-    __syncthreads();
-    const int64_t tile = s_tile;
-    if (tile >= n_tiles) return;
-    const int64_t base = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
-
-    double x[SCAN_ITEMS];
-    int head[SCAN_ITEMS];
-    int prev_curve = base > 0 && base - 1 < b.n_seg ? b.seg_curve[base - 1] : -1;
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) {
-        const int64_t s = base + k;
-        if (s < b.n_seg) {
-            x[k] = t.seg_len[s];
-            const int cc = b.seg_curve[s];
-            head[k] = (s == 0) || cc != prev_curve;
-            prev_curve = cc;
-        } else {
-            x[k] = 0.0;
-            head[k] = 0;
-        }
-    }
-    // thread aggregate
-    SegVal agg{0, DD{0.0, 0.0}};
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) agg = seg_combine(agg, SegVal{head[k], DD{x[k], 0.0}});
-    // warp inclusive scan of aggregates
-    SegVal inc = agg;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const SegVal y = shfl_up_sv(inc, d);
-        if (lane >= d) inc = seg_combine(y, inc);
-    }
-    if (lane == 31) s_warp[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        SegVal w = lane < SCAN_THREADS / 32 ? s_warp[lane] : SegVal{0, DD{0.0, 0.0}};
-#pragma unroll
-        for (int d = 1; d < SCAN_THREADS / 32; d <<= 1) {
-            const SegVal y = shfl_up_sv(w, d);
-            if (lane >= d) w = seg_combine(y, w);
-        }
-        if (lane < SCAN_THREADS / 32) s_warp[lane] = w;  // inclusive over warps
-    }
-    __syncthreads();
-    // exclusive prefix of this thread inside the tile
-    SegVal excl = shfl_up_sv(inc, 1);
-    if (lane == 0) excl = SegVal{0, DD{0.0, 0.0}};
-    if (warp > 0) excl = lane == 0 ? s_warp[warp - 1] : seg_combine(s_warp[warp - 1], excl);
-
-    // decoupled look-back by thread 0
-    if (threadIdx.x == 0) {
-        const SegVal tile_agg = s_warp[SCAN_THREADS / 32 - 1];
-        SegVal pre{0, DD{0.0, 0.0}};
-        if (tile == 0) {
-            pre = SegVal{1, DD{0.0, 0.0}};
-        } else {
-            t.scan_flag[tile] = tile_agg.flag;
-            t.scan_hi[tile] = tile_agg.v.hi;
-            t.scan_lo[tile] = tile_agg.v.lo;
-            __threadfence();
-            atomicExch(t.scan_status + tile, 1);
-            bool done = false;
-            for (int64_t j = tile - 1; j >= 0 && !done; --j) {
-                int st = 0;
-                for (long long it = 0; it < SCAN_SPIN_LIMIT; ++it) {
-                    st = atomicAdd(t.scan_status + j, 0);
-                    if (st) break;
-                    __nanosleep(64);
-                }
-                if (!st) {
-                    raise_err(t, ERR_SCAN_TIMEOUT);
-                    break;
-                }
-                __threadfence();
-                const SegVal pj{__ldcg(t.scan_flag + j), DD{__ldcg(t.scan_hi + j), __ldcg(t.scan_lo + j)}};
-                pre = seg_combine(pj, pre);
-                if (st == 2 || pj.flag) done = true;
-            }
-        }
-        const SegVal incl = seg_combine(pre, tile_agg);
-        t.scan_flag[tile] = 1;
-        t.scan_hi[tile] = incl.v.hi;
-        t.scan_lo[tile] = incl.v.lo;
-        __threadfence();
-        atomicExch(t.scan_status + tile, 2);
-        s_prefix = pre;
-    }
-    __syncthreads();
-    SegVal run = seg_combine(s_prefix, excl);
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) {
-        run = seg_combine(run, SegVal{head[k], DD{x[k], 0.0}});
-        const int64_t s = base + k;
-        if (s < b.n_seg) t.seg_cum[s] = run.v.hi + run.v.lo;
-    }
-}
-
-static __global__ void k_curve_len(Batch b, Table t)
-{
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < b.n_curve;
-         c += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t e = b.seg_off[c + 1];
-        t.curve_len[c] = e > b.seg_off[c] ? t.seg_cum[e - 1] : 0.0;
-    }
-}
-
 // ------------------------------------------------------------- sampling
 // One thread per sample: curve by binary search of the sample offsets,
 // segment by binary search of the cumulative segment table, leaf panel by
@@ -297,7 +94,32 @@ struct SampleParams {
     int64_t n_samples;
     int collect;
     double rtol;  // the table's tolerance: samples are placed to 1 % of rtol * L
+    // Batches that mix curve codes run one launch per code over the curves
+    // curve_list[cb .. ce) (grouped by code); list_off is the prefix of their
+    // sample counts in that order.  curve_list NULL: all samples, curve order.
+    const int* curve_list;
+    const int64_t* list_off;
+    int64_t cb, ce;
 };
+
+// Sample range of a launch and, for launch-local sample i, its curve and its
+// index gi in the caller's position / output arrays.
+__device__ __forceinline__ void sample_range(const SampleParams& P, int64_t& i0, int64_t& i1)
+{
+    i0 = P.curve_list ? P.list_off[P.cb] : 0;
+    i1 = P.curve_list ? P.list_off[P.ce] : P.n_samples;
+}
+__device__ __forceinline__ int sample_curve(const SampleParams& P, int64_t i, int64_t& gi)
+{
+    if (P.curve_list) {
+        const int64_t j = P.cb + upper_bound_i64(P.list_off + P.cb, int(P.ce - P.cb) + 1, i);
+        const int c = P.curve_list[j];
+        gi = P.sample_off[c] + (i - P.list_off[j]);
+        return c;
+    }
+    gi = i;
+    return upper_bound_i64(P.sample_off, int(P.b.n_curve) + 1, i);
+}
 
 constexpr int SAMPLE_THREADS = 256;
 constexpr int NEWTON_MAXIT = 16;
@@ -384,9 +206,12 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) k_sample(SampleParams P)
     const Batch& b = P.b;
     const Table& t = P.t;
     unsigned long long newton = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n_samples;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int c = upper_bound_i64(P.sample_off, int(b.n_curve) + 1, i);
+    int64_t i0, i1;
+    sample_range(P, i0, i1);
+    for (int64_t ii = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ii < i1;
+         ii += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i;
+        const int c = sample_curve(P, ii, i);
         const int code = CODE >= 0 ? CODE : curve_code(b, c);
         const int64_t s0 = b.seg_off[c], s1 = b.seg_off[c + 1];
         int64_t s;

@@ -106,9 +106,12 @@ __global__ void __launch_bounds__(SAMPLE_THREADS) k_sample_ff(SampleParams P, co
     const Batch& b = P.b;
     const Table& t = P.t;
     unsigned long long newton = 0;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.n_samples;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int c = upper_bound_i64(P.sample_off, int(b.n_curve) + 1, i);
+    int64_t i0, i1;
+    sample_range(P, i0, i1);
+    for (int64_t ii = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ii < i1;
+         ii += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i;
+        const int c = sample_curve(P, ii, i);
         const int code = CODE >= 0 ? CODE : curve_code(b, c);
         const int64_t s0 = b.seg_off[c], s1 = b.seg_off[c + 1];
         int64_t s;

@@ -65,6 +65,19 @@ struct Table {
     double* scan_lo;
 };
 
+// double-double value and its two-sum addition (compensated sums)
+struct DD {
+    double hi, lo;
+};
+__device__ __forceinline__ DD dd_add(DD a, DD b)
+{
+    const double s = a.hi + b.hi;
+    const double bb = s - a.hi;
+    double e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    const double h = s + e;
+    return DD{h, e - (h - s)};
+}
 __device__ __forceinline__ int curve_code(const Batch& b, int64_t c)
 {
     return b.kind[c] == 0 ? CODE_ELLIPSE : bs_code(b.degree[c], b.dim[c]);
