@@ -96,6 +96,22 @@ gcv_status upload(DBuf<T>& b, const T* h, size_t count, cudaStream_t st)
     return GCV_OK;
 }
 
+// Whether kernels may read and write pageable host memory directly (coherent
+// NVLink-C2C with the host's page tables, as on Grace-Blackwell).  Sampling
+// then streams host positions in and host results out inside the kernel,
+// overlapped with its arithmetic, instead of staging copies around it.
+bool pageable_access()
+{
+    static int v = -1;
+    if (v < 0) {
+        int dev = 0, a = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) a = 0;
+        v = a;
+    }
+    return v == 1;
+}
+
 int sm_count()
 {
     static int n = 0;
@@ -143,7 +159,8 @@ struct gcv_ctx {
     DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_q0, seg_len, seg_cum, curve_len;
     DBuf<int64_t> leaf_off;
     DBuf<int> leaf_cnt;
-    DBuf<double> leaf_v, leaf_cum, leaf_f, leaf_q;
+    DBuf<double> leaf_v, leaf_cum;
+    DBuf<float> leaf_f, leaf_q;
     int64_t leaf_cap = 0;
     DBuf<int> deep_list;
     DBuf<unsigned long long> ctr;
@@ -489,19 +506,26 @@ gcv_status ensure_table_buffers(gcv_ctx* c)
 }
 
 // grows the leaf pool to `cap`, keeping the first `keep` leaves
+template <typename T>
+gcv_status grow_buf(gcv_ctx* c, DBuf<T>& b, int64_t cap, int64_t keep)
+{
+    DBuf<T> nb;
+    CHECK(nb.reserve((size_t)cap));
+    if (keep > 0) CU(cudaMemcpyAsync(nb.p, b.p, (size_t)keep * sizeof(T), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    b.release();
+    b = nb;
+    nb.p = nullptr;
+    nb.n = 0;
+    return GCV_OK;
+}
+
 gcv_status grow_pool(gcv_ctx* c, int64_t cap, int64_t keep)
 {
-    DBuf<double>* bufs[4] = {&c->leaf_v, &c->leaf_cum, &c->leaf_f, &c->leaf_q};
-    for (DBuf<double>* b : bufs) {
-        DBuf<double> nb;
-        CHECK(nb.reserve((size_t)cap));
-        if (keep > 0) CU(cudaMemcpyAsync(nb.p, b->p, (size_t)keep * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
-        CU(cudaStreamSynchronize(c->stream));
-        b->release();
-        *b = nb;
-        nb.p = nullptr;
-        nb.n = 0;
-    }
+    CHECK(grow_buf(c, c->leaf_v, cap, keep));
+    CHECK(grow_buf(c, c->leaf_cum, cap, keep));
+    CHECK(grow_buf(c, c->leaf_f, cap, keep));
+    CHECK(grow_buf(c, c->leaf_q, cap, keep));
     c->leaf_cap = cap;
     return GCV_OK;
 }
@@ -1048,20 +1072,25 @@ gcv_status gcv_arclength_reverse_into(gcv_ctx* ctx, const int* n_ptrs_for_curves
     CHECK(stage_counts(ctx, n_ptrs_for_curves, in_where, &total));
     if (total == 0) return GCV_OK;
     if (!sample_position || !out) return fail(GCV_ERR_INVALID, "NULL positions or output");
+    // host buffers: read / written in place by the sampling kernels where the
+    // device has coherent pageable-memory access, else staged through device
+    // buffers
+    const bool direct = pageable_access();
     const double* d_pos = sample_position;
-    if (in_where == GCV_HOST) {
+    if (in_where == GCV_HOST && !direct) {
         CHECK(upload(ctx->sample_pos, sample_position, (size_t)total, ctx->stream));
         d_pos = ctx->sample_pos.p;
     }
     const int width = what == GCV_RETURN_US ? 1 : ctx->point_dim;
     double* d_out = out;
-    if (out_where == GCV_HOST) {
+    if (out_where == GCV_HOST && !direct) {
         CHECK(ctx->sample_out.reserve((size_t)total * width));
         d_out = ctx->sample_out.p;
     }
     CHECK(run_sampling(ctx, ctx->sample_off.p, d_pos, total, is_relative ? 1 : 0, what, d_out));
     if (out_where == GCV_HOST) {
-        CU(cudaMemcpyAsync(out, d_out, (size_t)total * width * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        if (!direct)
+            CU(cudaMemcpyAsync(out, d_out, (size_t)total * width * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
         CU(cudaStreamSynchronize(ctx->stream));
     }
     return GCV_OK;

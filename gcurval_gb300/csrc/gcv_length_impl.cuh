@@ -57,8 +57,8 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
 {
     __shared__ double lf_v[MODE == 0 ? LCAP : 1][LK_THREADS];
     __shared__ double lf_c[MODE == 0 ? LCAP : 1][LK_THREADS];
-    __shared__ double lf_f[MODE == 0 ? LCAP : 1][LK_THREADS];
-    __shared__ double lf_q[MODE == 0 ? LCAP : 1][LK_THREADS];
+    __shared__ float lf_f[MODE == 0 ? LCAP : 1][LK_THREADS];
+    __shared__ float lf_q[MODE == 0 ? LCAP : 1][LK_THREADS];
 
     const Batch& b = P.b;
     const Table& t = P.t;
@@ -78,6 +78,8 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
     unsigned long long k = 0;
     int depth = 0, nleaf = 0;
     double cum = 0.0, tol_unit = 0.0;
+    ff cumf{0.0f, 0.0f};  // float-float running sum (PREC 1)
+    float tol_f = 0.0f;
     long long panels = 0;
     unsigned long long my_panels = 0, my_capped = 0, my_nonfinite = 0;
 
@@ -115,6 +117,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                     depth = 0;
                     nleaf = 0;
                     cum = 0.0;
+                    cumf = ff{0.0f, 0.0f};
                     panels = 0;
                     if (MODE == 2) {
                         pool = (int64_t)atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)t.leaf_cnt[s]);
@@ -127,13 +130,13 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                         if (MODE == 0) {
                             lf_v[0][tid] = 1.0;
                             lf_c[0][tid] = 0.0;
-                            lf_f[0][tid] = 0.0;
-                            lf_q[0][tid] = 0.0;
+                            lf_f[0][tid] = 0.0f;
+                            lf_q[0][tid] = 0.0f;
                         } else if (MODE == 2 && pool >= 0) {
                             t.leaf_v[pool] = 1.0;
                             t.leaf_cum[pool] = 0.0;
-                            t.leaf_f[pool] = 0.0;
-                            t.leaf_q[pool] = 0.0;
+                            t.leaf_f[pool] = 0.0f;
+                            t.leaf_q[pool] = 0.0f;
                         }
                         nleaf = 1;
                         fin = true;
@@ -145,51 +148,78 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
         }
         // ---- one panel per active lane
         if (active) {
-            const double hw = pow2_neg(depth);
-            const double vlo = fma(__ull2double_rn(k), 2.0 * hw, -1.0);
-            double K, G, fend, qend;
+            // panel values: K15, the error test, and (for leaves) the right-end
+            // speed f and slope q in FP64; the float-float path keeps its
+            // values in FP32 pairs and touches FP64 only for leaves and for
+            // error tests that land within 1 % of the threshold
+            bool ok, finite;
+            double K = 0.0, fend = 0.0, qend = 0.0;
+            ff Kf{0.0f, 0.0f}, fendf{0.0f, 0.0f};
+            float q32 = 0.0f;
             if constexpr (PREC == 1) {
-                ff Kf, Gf, ff_end;
-                float q32;
+                ff Gf;
                 if constexpr (CODE >= 0)
-                    panel_k15_ff<(CODE >= 0 ? CODE : 0)>(rf, k, depth, Kf, Gf, ff_end, q32);
+                    panel_k15_ff<(CODE >= 0 ? CODE : 0)>(rf, k, depth, Kf, Gf, fendf, q32);
                 else
-                    panel_ff_dyn(code, rf, k, depth, Kf, Gf, ff_end, q32);
-                K = ff_to_double(Kf);
-                G = ff_to_double(Gf);
-                fend = ff_to_double(ff_end);
-                qend = (double)q32;
+                    panel_ff_dyn(code, rf, k, depth, Kf, Gf, fendf, q32);
+                if (depth == 0) {
+                    tol_unit = P.rtol * fabs(ff_to_double(Kf));
+                    tol_f = (float)tol_unit;
+                }
+                const ff dkg = ff_add(Kf, ff_neg(Gf));
+                const float hwf = __int_as_float((127 - depth) << 23);  // 2^-depth
+                const float errf = fabsf(dkg.hi);
+                const float thr = fmaxf(tol_f * hwf, (float)eps50 * fabsf(Kf.hi));
+                finite = isfinite(Kf.hi) && isfinite(Gf.hi);
+                if (errf < 0.99f * thr) {
+                    ok = true;
+                } else if (errf > 1.01f * thr && thr > 1e-30f) {
+                    ok = false;
+                } else {  // near the tolerance (or below FP32 range): the FP64 test
+                    const double Kd = ff_to_double(Kf);
+                    ok = fabs(ff_to_double(dkg)) <= fmax(tol_unit * pow2_neg(depth), eps50 * fabs(Kd));
+                }
             } else {
+                const double hw = pow2_neg(depth);
+                const double vlo = fma(__ull2double_rn(k), 2.0 * hw, -1.0);
+                double G;
                 if constexpr (CODE >= 0)
                     panel_k15<(CODE >= 0 ? CODE : 0)>(r, vlo, hw, K, G, fend, qend);
                 else
                     panel_dyn(code, r, vlo, hw, K, G, fend, qend);
+                if (depth == 0) tol_unit = P.rtol * fabs(K);
+                finite = isfinite(K) && isfinite(G);
+                ok = fabs(K - G) <= fmax(tol_unit * hw, eps50 * fabs(K));
             }
-            if (depth == 0) tol_unit = P.rtol * fabs(K);
             ++panels;
-            const double err = fabs(K - G);
-            const bool finite = isfinite(K) && isfinite(G);
             const bool at_cap = depth >= P.max_depth || panels >= PANEL_BUDGET;
-            const bool ok = err <= fmax(tol_unit * hw, eps50 * fabs(K));
             if (ok || at_cap || !finite) {
                 if (!ok && finite) ++my_capped;
                 if (!finite) ++my_nonfinite;
-                cum += K;
-                const double vr = vlo + 2.0 * hw;
+                if constexpr (PREC == 1) {
+                    cumf = ff_add(cumf, Kf);
+                    cum = ff_to_double(cumf);
+                    fend = ff_to_double(fendf);
+                    qend = (double)q32;
+                } else {
+                    cum += K;
+                }
+                // right end -1 + (k + 1) 2^(1 - depth): exact
+                const double vr = fma(__ull2double_rn(k + 1), 2.0 * pow2_neg(depth), -1.0);
                 if (MODE == 0) {
                     if (nleaf < LCAP) {
                         lf_v[nleaf][tid] = vr;
                         lf_c[nleaf][tid] = cum;
-                        lf_f[nleaf][tid] = fend;
-                        lf_q[nleaf][tid] = qend;
+                        lf_f[nleaf][tid] = (float)fend;
+                        lf_q[nleaf][tid] = (float)qend;
                     } else {
                         ovf = true;
                     }
                 } else if (MODE == 2) {
                     t.leaf_v[pool + nleaf] = vr;
                     t.leaf_cum[pool + nleaf] = cum;
-                    t.leaf_f[pool + nleaf] = fend;
-                    t.leaf_q[pool + nleaf] = qend;
+                    t.leaf_f[pool + nleaf] = (float)fend;
+                    t.leaf_q[pool + nleaf] = (float)qend;
                 }
                 ++nleaf;
                 ++k;

@@ -53,8 +53,8 @@ struct Table {
     int* leaf_cnt;
     double* leaf_v;    // right end (local v) of each leaf panel
     double* leaf_cum;  // cumulative length within the segment at that end
-    double* leaf_f;    // f at that end
-    double* leaf_q;    // f * df/dv at that end
+    float* leaf_f;     // f at that end (shapes the sampling guess only)
+    float* leaf_q;     // f * df/dv at that end
     int64_t leaf_cap;
     int* deep_list;
     int64_t deep_cap;

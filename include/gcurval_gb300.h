@@ -184,7 +184,11 @@ gcv_status gcv_arclength_reverse(gcv_ctx* ctx, const int* n_ptrs_for_curves,
 
 /* The same into caller-provided memory: counts and positions in `in_where`
  * memory, output `out` (n points or n * point_dim doubles) in `out_where`
- * memory.  No allocation for the result. */
+ * memory.  No allocation for the result.  On devices with coherent access
+ * to pageable host memory (cudaDevAttrPageableMemoryAccess, e.g. over
+ * NVLink-C2C) host positions and host outputs are read and written in place
+ * by the sampling kernels; elsewhere they are staged through device buffers.
+ * Either way the call returns after the results are in `out`. */
 gcv_status gcv_arclength_reverse_into(gcv_ctx* ctx, const int* n_ptrs_for_curves,
                                       const double* sample_position, int is_relative,
                                       int in_where, int what, double* out, int out_where);
