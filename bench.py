@@ -59,8 +59,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="uniform_bsplines")
-    ap.add_argument("--precision", choices=["plain", "mixed"], default="plain")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="uneven_batch")
+    ap.add_argument("--precision", choices=["plain", "mixed"], default="mixed")
+    ap.add_argument("--plain-steps", type=int, default=3,
+                    help="timed steps of the plain FP64 form on the same batch, for the speed-up (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-sample-curves", type=int, default=0, help="curves in the CPU-baseline sample (0: auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -144,27 +146,64 @@ def cpu_sample(batch, n_curves: int):
     return sub
 
 
+def _groups(batch):
+    """Curve subsets of one (kind, degree, dim): the reference's CPU driver
+    is instantiated per curve type, as its sample programs are."""
+    key = batch.kind.astype(np.int64) * 100 + batch.degree.astype(np.int64) * 10 + batch.dim.astype(np.int64)
+    return [batch.subset(np.nonzero(key == k)[0]) for k in np.unique(key)]
+
+
 def run_cpu_reference(sub, nthreads: int, prefer_reference: bool = True):
-    """One pass of the reference CPU algorithm over `sub`: (seconds, kind)."""
+    """One pass of the reference CPU algorithm over `sub` (table + sampling of
+    every sample): (seconds, kind).  Batches that mix curve types run one
+    reference calculator per type, back to back."""
     from oracle import oracle as orc
     if prefer_reference and orc.reference_available():
-        try:
-            ref = orc.Reference(sub, nthreads=nthreads)
-            t0 = time.perf_counter()
-            ref.run(sub.n_samples, sub.positions, True, 0)
-            return time.perf_counter() - t0, "reference"
-        except ValueError:
-            pass  # mixed kinds: the reference driver takes one kind per batch
+        parts = _groups(sub)
+        for p in parts:
+            p.sample_positions()
+        refs = [orc.Reference(p, nthreads=nthreads) for p in parts]
+        t0 = time.perf_counter()
+        for p, ref in zip(parts, refs):
+            ref.run(p.n_samples, p.positions, True, 0)
+        return time.perf_counter() - t0, "reference"
     t0 = time.perf_counter()
     o = orc.Oracle(sub, nthreads=nthreads)
     o.reverse(sub.n_samples, sub.positions, True, 0)
     return time.perf_counter() - t0, "port"
 
 
-def auto_cpu_curves(batch) -> int:
-    # about 10-20 s of single-thread CPU work, spread over the host threads
-    per_curve = 6e-3 * float(batch.n_segments.mean()) / 61.0 + 3.4e-6 * float(batch.n_samples.mean())
-    return int(max(16, min(batch.n_curve, 15.0 / max(per_curve, 1e-6))))
+def accuracy_vs_oracle(sub, precision, rtol):
+    """Relative total-length error and sample-position error |s(u) - target| / L
+    of the library on `sub` against the FP64 oracle (the reference's CPU
+    algorithm restated), maxima over the subset."""
+    import gcurval_gb300 as g
+    from oracle import oracle as orc
+    calc = g.ArclengthCalculateGpu.from_batch(sub, precision=precision, rtol=rtol)
+    try:
+        calc.createArclengthTable()
+        L = calc.getAllCurveArclengths()
+        u = calc.arclengthReverse(sub.n_samples, sub.positions, True, g.GCV_HOST).us
+    finally:
+        calc.close()
+    o = orc.Oracle(sub)
+    Lo = o.lengths()
+    s = o.s_at(sub.n_samples, u)
+    tgt = sub.positions * np.repeat(Lo, sub.n_samples)
+    Lrep = np.maximum(np.repeat(Lo, sub.n_samples), 1e-300)
+    return {"curves": int(sub.n_curve), "samples": int(sub.total_samples),
+            "max_rel_length_err": float(np.max(np.abs(L - Lo) / np.maximum(Lo, 1e-300))),
+            "max_rel_sample_err": float(np.max(np.abs(s - tgt) / Lrep)) if s.size else 0.0,
+            "oracle": "oracle/ C restatement of ArclengthCalculateCpu, FP64"}
+
+
+def auto_cpu_curves(batch, nthreads: int, target_s: float) -> int:
+    """Curves of the CPU sample: a pilot of 32 curves spread over the batch,
+    timed, scaled to about `target_s` seconds on `nthreads` threads."""
+    pilot = cpu_sample(batch, min(32, batch.n_curve))
+    secs, _ = run_cpu_reference(pilot, nthreads)
+    n = int(pilot.n_curve * target_s / max(secs, 1e-3))
+    return int(max(16, min(batch.n_curve, n)))
 
 
 # --------------------------------------------------------------- our arm
@@ -212,46 +251,62 @@ def main():
     d_pos = tk(pos, torch.float64)
     d_out = torch.empty(n_samples, dtype=torch.float64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-    calc = g.ArclengthCalculateGpu.from_device_batch(*d_arr, precision=precision, collect_stats=True)
 
-    def step():
-        calc.createArclengthTable()
-        calc.arclengthReverseInto(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
+    def device_arm(prec, steps, warmup, clocks=False):
+        """Times `steps` table builds + samplings of the resident batch with CUDA
+        events (L2 flushed before each); returns the per-step figures."""
+        calc = g.ArclengthCalculateGpu.from_device_batch(*d_arr, precision=prec, rtol=batch.rtol, collect_stats=True)
 
-    for _ in range(max(args.warmup, 3)):
-        step()
-    torch.cuda.synchronize()
-    st0 = calc.stats()
-    launches0 = st0["n_launches"]
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    ms_len, ms_samp, n_newton, n_panels = [], [], [], []
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        for i in range(args.steps):
-            flush.zero_()
-            evs[i][0].record()
+        def step():
+            calc.createArclengthTable()
+            calc.arclengthReverseInto(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
+
+        for _ in range(warmup):
             step()
-            evs[i][1].record()
-            s = calc.stats()  # synchronises; outside the events
-            ms_len.append(s["ms_length"])
-            ms_samp.append(s["ms_sample"])
-            n_newton.append(s["n_newton"])
-            n_panels.append(s["n_panels"])
         torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = float(sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    st1 = calc.stats()
-    launches = st1["n_launches"] - launches0
-    leaves = st1["n_leaves"]
-    ms_per_step = total_ms / args.steps
+        launches0 = calc.stats()["n_launches"]
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        r = {"ms_len": [], "ms_samp": [], "ms_setup": [], "n_newton": [], "n_panels": []}
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clk:
+            for i in range(steps):
+                flush.zero_()
+                evs[i][0].record()
+                step()
+                evs[i][1].record()
+                st = calc.stats()  # synchronises; outside the events
+                r["ms_len"].append(st["ms_length"])
+                r["ms_samp"].append(st["ms_sample"])
+                r["ms_setup"].append(st["ms_setup"] + st["ms_scan"])
+                r["n_newton"].append(st["n_newton"])
+                r["n_panels"].append(st["n_panels"])
+            torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        total_ms = float(sum(x.elapsed_time(y) for x, y in evs))
+        if dist:
+            t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            total_ms = float(t.item())
+        st1 = calc.stats()
+        r["launches"] = st1["n_launches"] - launches0
+        r["leaves"] = st1["n_leaves"]
+        r["deep"] = st1["n_deep_segments"]
+        r["ms_per_step"] = total_ms / steps
+        r["clocks"] = clk.summary() if clocks else None
+        calc.close()
+        return r
+
+    main_r = device_arm(precision, args.steps, max(args.warmup, 3), clocks=True)
+    plain_r = None
+    if precision != g.GCV_PLAIN_FP64 and args.plain_steps > 0:
+        plain_r = device_arm(g.GCV_PLAIN_FP64, args.plain_steps, 1)
+    ms_per_step = main_r["ms_per_step"]
+    launches = main_r["launches"]
+    leaves = main_r["leaves"]
+    ms_len, ms_samp, n_newton, n_panels = main_r["ms_len"], main_r["ms_samp"], main_r["n_newton"], main_r["n_panels"]
     value = world * n_curves / (ms_per_step * 1e-3)
     samples_per_s = world * n_samples / (ms_per_step * 1e-3)
 
@@ -293,14 +348,14 @@ def main():
         "hbm": {"achieved_gbs": round(bytes_alg / (ms * 1e-3) / 1e9, 2), "peak_gbs": hbm_peak,
                 "frac": round(bytes_alg / (ms * 1e-3) / 1e9 / hbm_peak, 4) if hbm_peak else None,
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
-        "phases_ms": {"length": round(ms_l, 4), "sample": round(ms_s, 4)},
+        "phases_ms": {"length": round(ms_l, 4), "sample": round(ms_s, 4),
+                      "setup_scan": round(float(np.mean(main_r["ms_setup"])), 4)},
         "work_per_step": {"panels": float(np.mean(n_panels)), "newton_iterations": float(np.mean(n_newton)),
                           "leaves": int(leaves), "segments": int(batch.n_segments.sum()),
                           "length_tflops": round(len_flops / (ms_l * 1e-3) / 1e12, 4),
                           "sample_tflops": round(samp_flops / (ms_s * 1e-3) / 1e12, 4)},
         "fp32_peak_tflops": round(fp32_peak, 2),
     }
-    calc.close()
 
     # ---- end-to-end through the public API with host buffers -----------------
     e2e_t = []
@@ -309,7 +364,7 @@ def main():
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
-        c2 = g.ArclengthCalculateGpu.from_batch(batch, precision=precision)
+        c2 = g.ArclengthCalculateGpu.from_batch(batch, precision=precision, rtol=batch.rtol)
         c2.createArclengthTable()
         c2.arclengthReverseInto(batch.n_samples, pos, h_out, True, g.GCV_RETURN_US)
         c2.close()
@@ -324,15 +379,26 @@ def main():
     h2d = batch.nbytes() + batch.n_samples.nbytes + pos.nbytes
     d2h = h_out.nbytes
 
-    # ---- CPU baseline (rank 0, N = 1 only) -----------------------------------
-    cpu = None
+    # ---- CPU baseline and accuracy (rank 0, N = 1 only) ----------------------
+    cpu = acc = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         nthreads = os.cpu_count() or 1
-        sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch))
+        sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch, nthreads, 10.0))
         secs, kind = run_cpu_reference(sub, nthreads)
         cpu = {"value": round(sub.n_curve / secs, 3), "unit": "curves/s", "cores": nthreads, "kind": kind,
                "sample": f"{sub.n_curve} curves of the workload ({sub.total_samples} samples), table + sampling, "
                          f"{secs:.2f} s", "samples_per_s": round(sub.total_samples / secs, 1)}
+        acc = accuracy_vs_oracle(sub, precision, batch.rtol)
+    plain = None
+    if plain_r is not None:
+        pv = world * n_curves / (plain_r["ms_per_step"] * 1e-3)
+        plain = {"value": round(pv, 3), "unit": "curves/s", "ms_per_step": round(plain_r["ms_per_step"], 4),
+                 "steps": args.plain_steps, "warmup": 1, "rtol": batch.rtol,
+                 "samples_per_s": round(world * n_samples / (plain_r["ms_per_step"] * 1e-3), 1),
+                 "phases_ms": {"length": round(float(np.mean(plain_r["ms_len"])), 4),
+                               "sample": round(float(np.mean(plain_r["ms_samp"])), 4),
+                               "setup_scan": round(float(np.mean(plain_r["ms_setup"])), 4)},
+                 "speedup_of_this_form": round(value / pv, 3)}
 
     if rank == 0:
         line = {
@@ -341,7 +407,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == g.GCV_PLAIN_FP64 else "f32+f64",
             "data": "synthetic: seeded generator (numpy default_rng, seed = rank)",
             "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][1]}",
-                       "precision": args.precision, "rtol": 1e-10 if precision == g.GCV_PLAIN_FP64 else 1e-8,
+                       "precision": args.precision, "rtol": batch.rtol,
                        "curves_per_gpu": n_curves, "samples_per_gpu": n_samples,
                        "l2": "flushed between timed steps (256 MB write, untimed)",
                        "parallelism": f"replicas x{world} (independent curves, no collective)"},
@@ -352,7 +418,9 @@ def main():
             "gpu_launches": int(launches),
             "roofline": roofline,
             "cpu_baseline": cpu,
-            "clocks": clk.summary(),
+            "accuracy_vs_fp64_oracle": acc,
+            "plain_fp64_same_batch": plain,
+            "clocks": main_r["clocks"],
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -362,7 +430,9 @@ def main():
 def reference_arm(args):
     nthreads = os.cpu_count() or 1
     batch = make_batch(args.workload, seed=0, n_curves=args.n_curves)
-    sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch))
+    # each step a bounded sample: the whole --steps / --warmup run stays within minutes
+    per_step_s = min(5.0, 150.0 / max(args.steps + max(args.warmup, 3), 1))
+    sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch, nthreads, per_step_s))
     times, kind = [], None
     for i in range(max(args.warmup, 3) + args.steps):
         secs, kind = run_cpu_reference(sub, nthreads)
