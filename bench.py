@@ -358,19 +358,24 @@ def main():
     }
 
     # ---- end-to-end through the public API with host buffers -----------------
-    e2e_t = []
-    h_out = np.empty(n_samples, np.float64)
+    e2e_t, parts = [], []
+    h_out = np.zeros(n_samples, np.float64)
     for i in range(max(args.e2e_steps, 1) + 1):
         if dist:
             dist.barrier()
-        t0 = time.perf_counter()
+        t = [time.perf_counter()]
         c2 = g.ArclengthCalculateGpu.from_batch(batch, precision=precision, rtol=batch.rtol)
+        t.append(time.perf_counter())
         c2.createArclengthTable()
+        t.append(time.perf_counter())
         c2.arclengthReverseInto(batch.n_samples, pos, h_out, True, g.GCV_RETURN_US)
+        t.append(time.perf_counter())
         c2.close()
-        dt = time.perf_counter() - t0
+        t.append(time.perf_counter())
         if i > 0:
-            e2e_t.append(dt)
+            e2e_t.append(t[-1] - t[0])
+            parts.append(np.diff(t) * 1e3)
+    e2e_parts = dict(zip(["create", "table", "sample", "destroy"], np.round(np.mean(parts, axis=0), 3).tolist()))
     e2e_s = float(np.mean(e2e_t))
     if dist:
         t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
@@ -414,7 +419,7 @@ def main():
             "samples_per_s": round(samples_per_s, 1),
             "e2e": {"value": round(world * n_curves / e2e_s, 3), "unit": "curves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "samples_per_s": round(world * n_samples / e2e_s, 1),
-                    "ms_per_step": round(e2e_s * 1e3, 3)},
+                    "ms_per_step": round(e2e_s * 1e3, 3), "breakdown_ms": e2e_parts},
             "gpu_launches": int(launches),
             "roofline": roofline,
             "cpu_baseline": cpu,

@@ -15,6 +15,7 @@
 
 #include "gcv_length.cuh"
 #include "gcv_sample.cuh"
+#include "gcv_staging.h"
 #include "gcv_table_kernels.cuh"
 
 using namespace gcv;
@@ -96,22 +97,6 @@ gcv_status upload(DBuf<T>& b, const T* h, size_t count, cudaStream_t st)
     return GCV_OK;
 }
 
-// Whether kernels may read and write pageable host memory directly (coherent
-// NVLink-C2C with the host's page tables, as on Grace-Blackwell).  Sampling
-// then streams host positions in and host results out inside the kernel,
-// overlapped with its arithmetic, instead of staging copies around it.
-bool pageable_access()
-{
-    static int v = -1;
-    if (v < 0) {
-        int dev = 0, a = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) a = 0;
-        v = a;
-    }
-    return v == 1;
-}
-
 int sm_count()
 {
     static int n = 0;
@@ -125,6 +110,8 @@ int sm_count()
 }
 
 }  // namespace
+
+constexpr int STREAM_EVENTS = 4;  // host-buffer sampling: events per stage, used round robin
 
 struct CodeRange {
     int code;
@@ -178,6 +165,9 @@ struct gcv_ctx {
     std::vector<double> h_len;
     bool h_len_valid = false;
     unsigned long long* h_ctr = nullptr;  // pinned
+    // chunked host <-> device streaming of samples
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    cudaEvent_t ev_in[STREAM_EVENTS] = {}, ev_done[STREAM_EVENTS] = {}, ev_out[STREAM_EVENTS] = {};
     gcv_stats stats{};
     cudaEvent_t ev[8] = {};
     bool ev_table = false, ev_sample = false;
@@ -285,6 +275,13 @@ void destroy_ctx(gcv_ctx* c)
     c->sample_out.release();
     c->coef_ff.release();
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
+    for (int k = 0; k < STREAM_EVENTS; ++k) {
+        if (c->ev_in[k]) cudaEventDestroy(c->ev_in[k]);
+        if (c->ev_done[k]) cudaEventDestroy(c->ev_done[k]);
+        if (c->ev_out[k]) cudaEventDestroy(c->ev_out[k]);
+    }
+    if (c->s_in) cudaStreamDestroy(c->s_in);
+    if (c->s_out) cudaStreamDestroy(c->s_out);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     delete c;
@@ -736,48 +733,141 @@ gcv_status launch_sampler(gcv_ctx* c, int code, const SampleParams& P, int64_t n
     return GCV_OK;
 }
 
-gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, const double* d_pos, int64_t total, int is_relative,
-                        int what, double* d_out)
+// sampling launches for the curves [c_lo, c_hi): one launch over their sample
+// range (uniform batch), or one per curve code over the part of that code's
+// grouped list (ascending curve ids) inside the range
+gcv_status launch_sample_chunk(gcv_ctx* c, SampleParams P, int64_t c_lo, int64_t c_hi, const std::vector<int64_t>& lo)
+{
+    if (c->code >= 0) {
+        P.curve_list = nullptr;
+        P.s_begin = c->h_sample_off[(size_t)c_lo];
+        P.s_end = c->h_sample_off[(size_t)c_hi];
+        if (P.s_end > P.s_begin) CHECK(launch_sampler(c, c->code, P, P.s_end - P.s_begin));
+        return GCV_OK;
+    }
+    P.curve_list = c->curve_list.p;
+    P.list_off = c->list_sample_off.p;
+    const int* L = c->h_curve_list.data();
+    for (const CodeRange& r : c->curve_ranges) {
+        const int64_t jb = std::lower_bound(L + r.begin, L + r.end, (int)c_lo) - L;
+        const int64_t je = std::lower_bound(L + r.begin, L + r.end, (int)c_hi) - L;
+        const int64_t ns = lo[(size_t)je] - lo[(size_t)jb];
+        if (ns == 0) continue;
+        P.cb = jb;
+        P.ce = je;
+        CHECK(launch_sampler(c, r.code, P, ns));
+    }
+    return GCV_OK;
+}
+
+gcv_status ensure_copy_streams(gcv_ctx* c)
+{
+    if (!c->s_in) CU(cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking));
+    if (!c->s_out) CU(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking));
+    for (int k = 0; k < STREAM_EVENTS; ++k) {
+        if (!c->ev_in[k]) CU(cudaEventCreateWithFlags(&c->ev_in[k], cudaEventDisableTiming));
+        if (!c->ev_done[k]) CU(cudaEventCreateWithFlags(&c->ev_done[k], cudaEventDisableTiming));
+        if (!c->ev_out[k]) CU(cudaEventCreateWithFlags(&c->ev_out[k], cudaEventDisableTiming));
+    }
+    return GCV_OK;
+}
+
+// Samples into d_out from positions d_pos.  Host buffers (h_pos, h_out,
+// either may be NULL) are streamed in chunks of curves through pinned
+// staging buffers: while chunk k is sampled, the host threads fill the
+// buffer of chunk k + 1 and drain the results of chunk k - 1, and the copy
+// engines move both over the link.
+gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, int64_t total, int is_relative,
+                        int what, double* d_out, const double* h_pos = nullptr, double* h_out = nullptr)
 {
     if (total == 0) return GCV_OK;
+    const int width = what == GCV_RETURN_US ? 1 : c->point_dim;
     CU(cudaEventRecord(c->ev[4], c->stream));
     if (c->opt.collect_stats) CU(cudaMemsetAsync(c->ctr.p + C_NEWTON, 0, sizeof(unsigned long long), c->stream));
-    {
-        SampleParams P;
-        P.b = batch_view(c);
-        P.t = table_view(c);
-        P.sample_off = d_sample_off;
-        P.pos = d_pos;
-        P.is_relative = is_relative;
-        P.what = what;
-        P.pdim = c->point_dim;
-        P.out = d_out;
-        P.n_samples = total;
-        P.collect = c->opt.collect_stats;
-        P.rtol = c->opt.rtol;
-        P.curve_list = nullptr;
-        P.list_off = nullptr;
-        P.cb = P.ce = 0;
-        if (c->code >= 0) {
-            CHECK(launch_sampler(c, c->code, P, total));
+    SampleParams P;
+    P.b = batch_view(c);
+    P.t = table_view(c);
+    P.sample_off = d_sample_off;
+    P.pos = d_pos;
+    P.is_relative = is_relative;
+    P.what = what;
+    P.pdim = c->point_dim;
+    P.out = d_out;
+    P.n_samples = total;
+    P.collect = c->opt.collect_stats;
+    P.rtol = c->opt.rtol;
+    P.curve_list = nullptr;
+    P.list_off = nullptr;
+    P.cb = P.ce = 0;
+    P.s_begin = 0;
+    P.s_end = total;
+    const int64_t n = c->n_curve;
+    std::vector<int64_t> lo;
+    if (c->code < 0) {
+        // sample-count prefix in grouped-list order
+        lo.assign((size_t)n + 1, 0);
+        for (int64_t j = 0; j < n; ++j) {
+            const int cj = c->h_curve_list[(size_t)j];
+            lo[(size_t)j + 1] = lo[(size_t)j] + (c->h_sample_off[(size_t)cj + 1] - c->h_sample_off[(size_t)cj]);
+        }
+        CHECK(upload(c->list_sample_off, lo.data(), lo.size(), c->stream));
+    }
+    if (!h_pos && !h_out) {
+        CHECK(launch_sample_chunk(c, P, 0, n, lo));
+    } else {
+        // chunks of whole curves of about STAGE_CHUNK bytes of positions
+        const int64_t per = (int64_t)(STAGE_CHUNK / sizeof(double));
+        std::vector<int64_t> cut{0};
+        while (cut.back() < n) {
+            const int64_t want = c->h_sample_off[(size_t)cut.back()] + per;
+            int64_t ci = std::upper_bound(c->h_sample_off.begin(), c->h_sample_off.end(), want) - c->h_sample_off.begin() - 1;
+            ci = std::min<int64_t>(std::max<int64_t>(ci, cut.back() + 1), n);
+            cut.push_back(ci);
+        }
+        const int chunks = (int)cut.size() - 1;
+        int64_t max_s = 0;
+        for (int k = 0; k < chunks; ++k)
+            max_s = std::max<int64_t>(max_s, c->h_sample_off[(size_t)cut[(size_t)k + 1]] - c->h_sample_off[(size_t)cut[(size_t)k]]);
+        CHECK(ensure_copy_streams(c));
+        auto lock = staging_lock();
+        void* slot[STAGE_SLOTS];
+        for (int i = 0; i < STAGE_SLOTS; ++i) {
+            const size_t bytes = (size_t)std::max<int64_t>(max_s, 1) * sizeof(double) * (i < 2 ? 1 : width);
+            cudaError_t e = staging_slot(i, bytes, &slot[i]);
+            if (e != cudaSuccess) return cuda_fail(e, "pinned staging buffer");
+        }
+        auto s_of = [&](int k) { return c->h_sample_off[(size_t)cut[(size_t)k]]; };
+        auto drain = [&](int k) -> gcv_status {  // results of chunk k -> caller
+            CU(cudaEventSynchronize(c->ev_out[k % STREAM_EVENTS]));
+            host_copy(h_out + s_of(k) * width, slot[2 + k % 2], (size_t)(s_of(k + 1) - s_of(k)) * width * sizeof(double));
+            return GCV_OK;
+        };
+        for (int k = 0; k < chunks; ++k) {
+            const int64_t s0 = s_of(k), s1 = s_of(k + 1);
+            const int e = k % STREAM_EVENTS;
+            if (h_pos && s1 > s0) {
+                if (k >= 2) CU(cudaEventSynchronize(c->ev_in[(k - 2) % STREAM_EVENTS]));  // buffer k % 2 is free
+                host_copy(slot[k % 2], h_pos + s0, (size_t)(s1 - s0) * sizeof(double));
+                CU(cudaMemcpyAsync(d_pos + s0, slot[k % 2], (size_t)(s1 - s0) * sizeof(double), cudaMemcpyHostToDevice,
+                                   c->s_in));
+                CU(cudaEventRecord(c->ev_in[e], c->s_in));
+                CU(cudaStreamWaitEvent(c->stream, c->ev_in[e], 0));
+            }
+            CHECK(launch_sample_chunk(c, P, cut[(size_t)k], cut[(size_t)k + 1], lo));
+            CU(cudaEventRecord(c->ev_done[e], c->stream));
+            if (h_out) {
+                // buffer 2 + k % 2 was drained on the host before this point
+                CU(cudaStreamWaitEvent(c->s_out, c->ev_done[e], 0));
+                CU(cudaMemcpyAsync(slot[2 + k % 2], d_out + s0 * width, (size_t)(s1 - s0) * width * sizeof(double),
+                                   cudaMemcpyDeviceToHost, c->s_out));
+                CU(cudaEventRecord(c->ev_out[e], c->s_out));
+                if (k >= 1) CHECK(drain(k - 1));
+            }
+        }
+        if (h_out) {
+            CHECK(drain(chunks - 1));
         } else {
-            // one launch per curve code over the grouped curve list
-            const int64_t n = c->n_curve;
-            std::vector<int64_t> lo((size_t)n + 1, 0);
-            for (int64_t j = 0; j < n; ++j) {
-                const int cj = c->h_curve_list[(size_t)j];
-                lo[(size_t)j + 1] = lo[(size_t)j] + (c->h_sample_off[(size_t)cj + 1] - c->h_sample_off[(size_t)cj]);
-            }
-            CHECK(upload(c->list_sample_off, lo.data(), lo.size(), c->stream));
-            P.curve_list = c->curve_list.p;
-            P.list_off = c->list_sample_off.p;
-            for (const CodeRange& r : c->curve_ranges) {
-                const int64_t ns = lo[(size_t)r.end] - lo[(size_t)r.begin];
-                if (ns == 0) continue;
-                P.cb = r.begin;
-                P.ce = r.end;
-                CHECK(launch_sampler(c, r.code, P, ns));
-            }
+            CU(cudaStreamSynchronize(c->s_in));
         }
     }
     CU(cudaEventRecord(c->ev[5], c->stream));
@@ -1072,27 +1162,22 @@ gcv_status gcv_arclength_reverse_into(gcv_ctx* ctx, const int* n_ptrs_for_curves
     CHECK(stage_counts(ctx, n_ptrs_for_curves, in_where, &total));
     if (total == 0) return GCV_OK;
     if (!sample_position || !out) return fail(GCV_ERR_INVALID, "NULL positions or output");
-    // host buffers: read / written in place by the sampling kernels where the
-    // device has coherent pageable-memory access, else staged through device
-    // buffers
-    const bool direct = pageable_access();
-    const double* d_pos = sample_position;
-    if (in_where == GCV_HOST && !direct) {
-        CHECK(upload(ctx->sample_pos, sample_position, (size_t)total, ctx->stream));
+    // host buffers are streamed through device buffers in chunks, overlapped
+    // with the sampling kernels
+    const int width = what == GCV_RETURN_US ? 1 : ctx->point_dim;
+    double* d_pos = const_cast<double*>(sample_position);
+    if (in_where == GCV_HOST) {
+        CHECK(ctx->sample_pos.reserve((size_t)total));
         d_pos = ctx->sample_pos.p;
     }
-    const int width = what == GCV_RETURN_US ? 1 : ctx->point_dim;
     double* d_out = out;
-    if (out_where == GCV_HOST && !direct) {
+    if (out_where == GCV_HOST) {
         CHECK(ctx->sample_out.reserve((size_t)total * width));
         d_out = ctx->sample_out.p;
     }
-    CHECK(run_sampling(ctx, ctx->sample_off.p, d_pos, total, is_relative ? 1 : 0, what, d_out));
-    if (out_where == GCV_HOST) {
-        if (!direct)
-            CU(cudaMemcpyAsync(out, d_out, (size_t)total * width * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-        CU(cudaStreamSynchronize(ctx->stream));
-    }
+    CHECK(run_sampling(ctx, ctx->sample_off.p, d_pos, total, is_relative ? 1 : 0, what, d_out,
+                       in_where == GCV_HOST ? sample_position : nullptr, out_where == GCV_HOST ? out : nullptr));
+    if (out_where == GCV_HOST) CU(cudaStreamSynchronize(ctx->stream));
     return GCV_OK;
 }
 

@@ -100,14 +100,15 @@ struct SampleParams {
     const int* curve_list;
     const int64_t* list_off;
     int64_t cb, ce;
+    int64_t s_begin, s_end;  // sample range of the launch when curve_list is NULL
 };
 
 // Sample range of a launch and, for launch-local sample i, its curve and its
 // index gi in the caller's position / output arrays.
 __device__ __forceinline__ void sample_range(const SampleParams& P, int64_t& i0, int64_t& i1)
 {
-    i0 = P.curve_list ? P.list_off[P.cb] : 0;
-    i1 = P.curve_list ? P.list_off[P.ce] : P.n_samples;
+    i0 = P.curve_list ? P.list_off[P.cb] : P.s_begin;
+    i1 = P.curve_list ? P.list_off[P.ce] : P.s_end;
 }
 __device__ __forceinline__ int sample_curve(const SampleParams& P, int64_t i, int64_t& gi)
 {

@@ -14,9 +14,10 @@
  *               (samples/sample1_ellipse/ellipse.h);
  *   - B-splines of degree 1..5 in 2D or 3D over their knot vector, one knot
  *               interval per segment (samples/sample2_bspline/).
- * User-defined curve functors go through the C++ header
- * include/gcurval/arclength_calculate.h, which instantiates the same kernels
- * on the user's plugin types.
+ * User-defined curve functors go through the header-only C++ path
+ * include/gcurval_gb300/gcurval.cuh (ArclengthCalculateGpu<Curve, CurveTraits>),
+ * whose kernels run the same adaptive walk, scan and Newton sampling
+ * instantiated on the user's plugin types.
  *
  * Errors: every entry point returns a gcv_status; gcv_last_error() gives a
  * message for the calling thread.  The reference instead calls exit(-1) in
@@ -184,11 +185,10 @@ gcv_status gcv_arclength_reverse(gcv_ctx* ctx, const int* n_ptrs_for_curves,
 
 /* The same into caller-provided memory: counts and positions in `in_where`
  * memory, output `out` (n points or n * point_dim doubles) in `out_where`
- * memory.  No allocation for the result.  On devices with coherent access
- * to pageable host memory (cudaDevAttrPageableMemoryAccess, e.g. over
- * NVLink-C2C) host positions and host outputs are read and written in place
- * by the sampling kernels; elsewhere they are staged through device buffers.
- * Either way the call returns after the results are in `out`. */
+ * memory.  No allocation for the result.  Host positions and host outputs
+ * are streamed through device buffers in chunks of curves, the copies of
+ * neighbouring chunks overlapping the sampling of the current one; the call
+ * returns after the results are in `out`. */
 gcv_status gcv_arclength_reverse_into(gcv_ctx* ctx, const int* n_ptrs_for_curves,
                                       const double* sample_position, int is_relative,
                                       int in_where, int what, double* out, int out_where);

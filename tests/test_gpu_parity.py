@@ -308,3 +308,22 @@ def test_full_size_ellipses_4096x1000(gpu_lib):
 def test_full_size_uniform_bsplines_10000x1024(gpu_lib):
     calc = _full_size_checks(ds.uniform_bsplines(10000, n_samples=1024, seed=0), n_check=200)
     assert calc.stats()["n_segments"] == 10000 * 61
+
+
+def test_host_buffers_stream_in_chunks_like_device_buffers(gpu_lib):
+    # more than one 256 MB chunk of positions, curves of every code: the
+    # chunked host pipeline must give the device path's results bit for bit
+    torch = pytest.importorskip("torch")
+    b = ds.uneven_batch(40000, seed=11)
+    pos = b.sample_positions()
+    assert b.total_samples * 8 > (256 << 20)
+    calc = g.ArclengthCalculateGpu.from_batch(b, precision=g.GCV_MIXED)
+    calc.createArclengthTable()
+    h_out = np.zeros(b.total_samples)
+    calc.arclengthReverseInto(b.n_samples, pos, h_out, True, g.GCV_RETURN_US)
+    d_cnt = torch.from_numpy(b.n_samples.astype(np.int32)).cuda()
+    d_pos = torch.from_numpy(pos).cuda()
+    d_out = torch.empty(b.total_samples, dtype=torch.float64, device="cuda")
+    calc.arclengthReverseInto(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
+    np.testing.assert_array_equal(h_out, d_out.cpu().numpy())
+    calc.close()

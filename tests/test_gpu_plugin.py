@@ -1,0 +1,113 @@
+"""The header-only plugin path (include/gcurval_gb300/gcurval.cuh): user-defined
+curve families through the reference's ArclengthCalculateGpu<Curve, CurveTraits>
+API, built by nvcc from tests/plugin/plugin_driver.cu and checked against the
+oracle (lengths, sample positions, points)."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from gcurval_gb300 import datasets as ds
+from oracle import oracle as orc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="session")
+def driver(tmp_path_factory):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = str(tmp_path_factory.mktemp("plugin") / "plugin_driver")
+    cmd = [nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+           "-o", exe, os.path.join(ROOT, "tests", "plugin", "plugin_driver.cu")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def run(driver, tmp_path, family, payload, n, total, what):
+    fin, fout = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    with open(fin, "wb") as f:
+        f.write(np.array([n, what], np.int32).tobytes())
+        for a in payload:
+            f.write(np.ascontiguousarray(a).tobytes())
+    r = subprocess.run([driver, family, fin, fout], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    out = np.fromfile(fout, np.float64)
+    L = out[:n]
+    rest = out[n:]
+    return L, (rest if what == 0 else rest.reshape(total, 2))
+
+
+def sample_err(o, batch, u, L):
+    s = o.s_at(batch.n_samples, u)
+    tgt = batch.positions * np.repeat(L, batch.n_samples)
+    return np.max(np.abs(s - tgt) / np.repeat(L, batch.n_samples))
+
+
+def ellipse_payload(b):
+    prm = b.ctrl.reshape(-1, 5)
+    return [prm[:, 0].copy(), prm[:, 1].copy(), b.n_samples.astype(np.int32), b.positions]
+
+
+def test_plugin_ellipses_lengths_and_samples(driver, tmp_path):
+    b = ds.ellipses(300, n_samples=33, seed=5)
+    b.sample_positions()
+    L, u = run(driver, tmp_path, "ellipse", ellipse_payload(b), b.n_curve, b.total_samples, 0)
+    o = orc.Oracle(b)
+    Lo = o.lengths()
+    assert np.max(np.abs(L - Lo) / Lo) <= 1e-10
+    assert sample_err(o, b, u, Lo) <= 1e-10
+    assert np.all((u >= 0) & (u <= 2 * np.pi))
+
+
+def test_plugin_ellipse_points(driver, tmp_path):
+    b = ds.ellipses(40, n_samples=9, seed=6)
+    b.sample_positions()
+    _, u = run(driver, tmp_path, "ellipse", ellipse_payload(b), b.n_curve, b.total_samples, 0)
+    _, pts = run(driver, tmp_path, "ellipse", ellipse_payload(b), b.n_curve, b.total_samples, 1)
+    prm = np.repeat(b.ctrl.reshape(-1, 5), b.n_samples, axis=0)
+    exp = np.stack([prm[:, 0] * np.cos(u), prm[:, 1] * np.sin(u)], axis=1)
+    np.testing.assert_allclose(pts, exp, rtol=0, atol=1e-12 * np.max(np.abs(exp)))
+
+
+def bspline_payload(b):
+    return [b.knot_off.astype(np.int32), b.knots, b.ctrl, b.n_samples.astype(np.int32), b.positions]
+
+
+def ragged_cubic_2d(n, seed):
+    """Cubic planar B-splines with 4-40 control points and clamped knots whose
+    interior values are sorted uniform draws (ragged interval counts)."""
+    rng = np.random.default_rng(seed)
+    knots, ctrl, klen, clen = [], [], [], []
+    for _ in range(n):
+        m = int(rng.integers(4, 41))
+        inner = np.sort(rng.random(m - 4))
+        kv = np.concatenate([np.zeros(4), inner, np.ones(4)])
+        pts = np.cumsum(rng.normal(size=(m, 2)) ** 2, axis=0)
+        knots.append(kv)
+        ctrl.append(pts.reshape(-1))
+        klen.append(kv.size)
+        clen.append(pts.size)
+    ko = np.concatenate([[0], np.cumsum(klen)]).astype(np.int64)
+    co = np.concatenate([[0], np.cumsum(clen)]).astype(np.int64)
+    ns = rng.integers(0, 50, n).astype(np.int32)
+    return ds.CurveBatch(np.ones(n, np.uint8), np.full(n, 3, np.uint8), np.full(n, 2, np.uint8), ko,
+                         np.concatenate(knots), co, np.concatenate(ctrl), ns, None, "ragged", 1e-10)
+
+
+@pytest.mark.parametrize("maker", ["uniform", "ragged"])
+def test_plugin_bsplines_through_shared_memory_hook(driver, tmp_path, maker):
+    b = ds.uniform_bsplines(200, n_ctrl=24, n_samples=17, seed=7) if maker == "uniform" else ragged_cubic_2d(150, 8)
+    b.sample_positions()
+    L, u = run(driver, tmp_path, "bspline", bspline_payload(b), b.n_curve, b.total_samples, 0)
+    o = orc.Oracle(b)
+    Lo = o.lengths()
+    assert np.max(np.abs(L - Lo) / Lo) <= 1e-10
+    assert sample_err(o, b, u, Lo) <= 1e-10
+    _, pts = run(driver, tmp_path, "bspline", bspline_payload(b), b.n_curve, b.total_samples, 1)
+    cid = np.repeat(np.arange(b.n_curve), b.n_samples)
+    for i in range(0, b.total_samples, max(1, b.total_samples // 60)):
+        np.testing.assert_allclose(pts[i], o.point(int(cid[i]), float(u[i]))[:2], rtol=1e-12, atol=1e-12)
