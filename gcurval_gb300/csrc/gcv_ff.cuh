@@ -81,6 +81,15 @@ __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return ff{a.hi * pow2
 // a * b + c
 __device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) { return ff_add(ff_mul(a, b), c); }
 
+// 1 / b: y = rcp(b.hi), then one Newton step y + y (1 - b y) with the
+// residual 1 - b y formed by FMAs (b.lo enters there)
+__device__ __forceinline__ ff ff_recip(ff b)
+{
+    const float y = __frcp_rn(b.hi);
+    const float e = fmaf(-b.lo, y, fmaf(-b.hi, y, 1.0f));
+    return fast_two_sum(y, __fmul_rn(y, e));
+}
+
 // sqrt: s = a * rsqrt(a) (a few ulp), then one Newton correction
 // s + (a - s^2) / (2 s) with the residual a - s^2 formed exactly by an FMA.
 __device__ __forceinline__ ff ff_sqrt(ff a)

@@ -142,6 +142,77 @@ struct EvalFF {
     }
 };
 
+// ------------------------------------------- symbolic de Boor set-up (FF)
+// bspline_setup (gcv_device.cuh) in float-float arithmetic, for tables built
+// for the mixed path: the same polynomial recursion in v on the FP32 pipes.
+// FP64 is used only to centre the data: knots relative to the span midpoint
+// m and control points relative to the first one of the span (differences
+// that carry the cancellation), each converted once to float-float.
+template <int P, int D>
+__device__ void bspline_setup_ff(const double* __restrict__ kv, const double* __restrict__ cp, int span, float2* out)
+{
+    const double ka = kv[span], kb = kv[span + 1];
+    const double m = 0.5 * (ka + kb);
+    const ff w = ff_from_double(0.5 * (kb - ka));
+    // knots span-P+1 .. span+P relative to m
+    ff dk[2 * P];
+#pragma unroll
+    for (int i = 0; i < 2 * P; ++i) dk[i] = ff_from_double(kv[span - P + 1 + i] - m);
+    // N[r][k]: basis polynomial r, coefficient of v^k
+    ff N[P + 1][P + 1];
+    N[0][0] = ff{1.0f, 0.0f};
+#pragma unroll
+    for (int j = 1; j <= P; ++j) {
+        ff saved[P + 1];
+#pragma unroll
+        for (int r = 0; r < j; ++r) {
+            const ff ra = dk[r + P];                // k[span + r + 1] - m
+            const ff la = ff_neg(dk[r + P - j]);    // m - k[span + 1 - j + r]
+            const ff inv = ff_recip(ff_add(ra, la));
+            ff temp[P + 1];
+#pragma unroll
+            for (int k = 0; k < j; ++k) temp[k] = ff_mul(N[r][k], inv);
+#pragma unroll
+            for (int k = j; k >= 0; --k) {
+                const ff a = r == 0 ? ff{0.0f, 0.0f} : saved[k];
+                if (k == j) {
+                    const ff wt = ff_mul(w, temp[k - 1]);
+                    N[r][k] = r == 0 ? ff_neg(wt) : ff_add(a, ff_neg(wt));
+                    saved[k] = wt;
+                } else if (k == 0) {
+                    const ff rt = ff_mul(ra, temp[0]);
+                    N[r][k] = r == 0 ? rt : ff_add(a, rt);
+                    saved[k] = ff_mul(la, temp[0]);
+                } else {
+                    const ff wt = ff_mul(w, temp[k - 1]);
+                    const ff rt = ff_add(ff_mul(ra, temp[k]), ff_neg(wt));
+                    N[r][k] = r == 0 ? rt : ff_add(a, rt);
+                    saved[k] = ff_add(ff_mul(la, temp[k]), wt);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k <= j; ++k) N[j][k] = saved[k];
+    }
+    // C(v) = P_0 + sum_{i >= 1} (P_i - P_0) N_i(v)  (the basis sums to one)
+    const double* c0 = cp + (size_t)(span - P) * D;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const double q = c0[d];
+        ff dp[P];
+#pragma unroll
+        for (int i = 1; i <= P; ++i) dp[i - 1] = ff_from_double(c0[i * D + d] - q);
+#pragma unroll
+        for (int k = 0; k <= P; ++k) {
+            ff acc{0.0f, 0.0f};
+#pragma unroll
+            for (int i = 1; i <= P; ++i) acc = i == 1 ? ff_mul(dp[0], N[1][k]) : ff_fma(dp[i - 1], N[i][k], acc);
+            if (k == 0) acc = ff_from_double(q + ff_to_double(acc));
+            out[k * D + d] = make_float2(acc.hi, acc.lo);
+        }
+    }
+}
+
 // float-float panel: K15, G7, right-end speed and slope of [vlo, vlo + 2 hw]
 // with vlo = -1 + k 2^(1-depth) built exactly from the integer k.
 template <int CODE>

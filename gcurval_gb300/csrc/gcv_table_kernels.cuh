@@ -4,9 +4,51 @@
 // totals.  Included by gcv_api.cu only.
 #pragma once
 
+#include "gcv_ff_eval.cuh"
 #include "gcv_kernels.cuh"
 
 namespace gcv {
+
+// set-up of one B-spline interval for a mixed-path table: float-float
+// coefficients straight from the float-float recursion
+template <int P, int D>
+__device__ void setup_bspline_seg_ff(const Batch& b, const Table& t, int64_t s, int64_t c)
+{
+    constexpr int N = code_stride(bs_code(P, D));
+    const int64_t j = s - b.seg_off[c];
+    const double* kv = b.knots + b.knot_off[c];
+    const double* cp = b.ctrl + b.ctrl_off[c];
+    const int span = int(j) + P;
+    float2* at = t.coef_ff + b.coef_off[c] + j * N;
+    const double ka = kv[span], kb = kv[span + 1];
+    if (!(kb >= ka)) raise_err(t, ERR_BAD_KNOTS);
+    if (kb > ka) {
+        bspline_setup_ff<P, D>(kv, cp, span, at);
+        t.seg_t0[s] = ka;
+        t.seg_t1[s] = kb;
+        ff r[P * D];
+        float q0;
+        EvalFF<bs_code(P, D)>::load(at, r);
+        t.seg_f0[s] = ff_to_double(EvalFF<bs_code(P, D)>::speed_slope(r, ff{-1.0f, 0.0f}, q0));
+        t.seg_q0[s] = (double)q0;
+    } else {
+#pragma unroll
+        for (int i = 0; i < N; ++i) at[i] = make_float2(0.0f, 0.0f);
+        t.seg_t0[s] = ka;
+        t.seg_t1[s] = ka;
+        t.seg_f0[s] = 0.0;
+        t.seg_q0[s] = 0.0;
+    }
+}
+
+template <int P, int D>
+__device__ __forceinline__ void setup_bspline_any(const Batch& b, const Table& t, int64_t s, int64_t c)
+{
+    if (t.coef_ff)
+        setup_bspline_seg_ff<P, D>(b, t, s, c);
+    else
+        setup_bspline_seg<P, D>(b, t, s, c);
+}
 
 static __global__ void k_setup(Batch b, Table t)
 {
@@ -16,7 +58,7 @@ static __global__ void k_setup(Batch b, Table t)
         switch (curve_code(b, c)) {
         case CODE_ELLIPSE: setup_ellipse_seg(b, t, s, c); break;
 #define GCV_SETUP_CASE(P, D)                                                                       \
-    case bs_code(P, D): setup_bspline_seg<P, D>(b, t, s, c); break;
+    case bs_code(P, D): setup_bspline_any<P, D>(b, t, s, c); break;
             GCV_SETUP_CASE(1, 2) GCV_SETUP_CASE(2, 2) GCV_SETUP_CASE(3, 2) GCV_SETUP_CASE(4, 2)
             GCV_SETUP_CASE(5, 2) GCV_SETUP_CASE(1, 3) GCV_SETUP_CASE(2, 3) GCV_SETUP_CASE(3, 3)
             GCV_SETUP_CASE(4, 3) GCV_SETUP_CASE(5, 3)
@@ -36,7 +78,7 @@ __global__ void k_setup_list(Batch b, Table t, const int* __restrict__ list, int
         if constexpr (CODE == CODE_ELLIPSE)
             setup_ellipse_seg(b, t, s, c);
         else
-            setup_bspline_seg<code_degree(CODE), code_dim(CODE)>(b, t, s, c);
+            setup_bspline_any<code_degree(CODE), code_dim(CODE)>(b, t, s, c);
     }
 }
 
@@ -77,7 +119,7 @@ static __global__ void k_deep_total(const int* __restrict__ list, int64_t n, con
 // replacing the reference's per-segment Brent-Kung scan plus one thread per
 // curve doing a sequential Kahan sum (gcurval/detail/cuda/kernel/generic.inl.cuh:52-137).
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr long long SCAN_SPIN_LIMIT = 1ll << 22;
 
@@ -112,26 +154,28 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, 
     if (tile >= n_tiles) return;
     const int64_t base = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
 
-    double x[SCAN_ITEMS];
-    int head[SCAN_ITEMS];
+    // Within a thread: plain FP64 running sums of at most SCAN_ITEMS lengths
+    // since the last curve start (rounding <= 16 ulp of the partial sum);
+    // across threads, tiles and the look-back: double-double.
+    double part[SCAN_ITEMS];  // running sum since the last start within the thread
+    unsigned heads = 0;       // bit k: item k starts a curve
     int prev_curve = base > 0 && base - 1 < b.n_seg ? b.seg_curve[base - 1] : -1;
+    double run = 0.0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
         const int64_t s = base + k;
+        double x = 0.0;
         if (s < b.n_seg) {
-            x[k] = t.seg_len[s];
+            x = t.seg_len[s];
             const int cc = b.seg_curve[s];
-            head[k] = (s == 0) || cc != prev_curve;
+            if (s == 0 || cc != prev_curve) heads |= 1u << k;
             prev_curve = cc;
-        } else {
-            x[k] = 0.0;
-            head[k] = 0;
         }
+        run = (heads >> k) & 1u ? x : run + x;
+        part[k] = run;
     }
     // thread aggregate
-    SegVal agg{0, DD{0.0, 0.0}};
-#pragma unroll
-    for (int k = 0; k < SCAN_ITEMS; ++k) agg = seg_combine(agg, SegVal{head[k], DD{x[k], 0.0}});
+    const SegVal agg{heads != 0, DD{run, 0.0}};
     // warp inclusive scan of aggregates
     SegVal inc = agg;
 #pragma unroll
@@ -195,12 +239,13 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, 
         s_prefix = pre;
     }
     __syncthreads();
-    SegVal run = seg_combine(s_prefix, excl);
+    // items before the thread's first curve start add the exclusive prefix
+    const SegVal pre = seg_combine(s_prefix, excl);
+    const int first_head = heads ? __ffs(heads) - 1 : SCAN_ITEMS;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
-        run = seg_combine(run, SegVal{head[k], DD{x[k], 0.0}});
         const int64_t s = base + k;
-        if (s < b.n_seg) t.seg_cum[s] = run.v.hi + run.v.lo;
+        if (s < b.n_seg) t.seg_cum[s] = k < first_head ? pre.v.hi + (pre.v.lo + part[k]) : part[k];
     }
 }
 
