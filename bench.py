@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="uneven_batch")
-    ap.add_argument("--precision", choices=["plain", "mixed"], default="mixed")
+    ap.add_argument("--precision", choices=["plain", "mixed", "learned"], default="mixed",
+                    help="plain FP64, mixed precision, or mixed precision with the learned start depths")
     ap.add_argument("--plain-steps", type=int, default=3,
                     help="timed steps of the plain FP64 form on the same batch, for the speed-up (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -173,13 +174,15 @@ def run_cpu_reference(sub, nthreads: int, prefer_reference: bool = True):
     return time.perf_counter() - t0, "port"
 
 
-def accuracy_vs_oracle(sub, precision, rtol):
+def accuracy_vs_oracle(sub, precision, rtol, model=None):
     """Relative total-length error and sample-position error |s(u) - target| / L
     of the library on `sub` against the FP64 oracle (the reference's CPU
     algorithm restated), maxima over the subset."""
     import gcurval_gb300 as g
     from oracle import oracle as orc
-    calc = g.ArclengthCalculateGpu.from_batch(sub, precision=precision, rtol=rtol)
+    calc = g.ArclengthCalculateGpu.from_batch(sub, precision=precision, rtol=rtol, learned=model is not None)
+    if model is not None:
+        calc.set_learned_model(model)
     try:
         calc.createArclengthTable()
         L = calc.getAllCurveArclengths()
@@ -237,7 +240,12 @@ def main():
     import gcurval_gb300 as g
     from gcurval_gb300 import _lib
 
-    precision = g.GCV_MIXED if args.precision == "mixed" else g.GCV_PLAIN_FP64
+    precision = g.GCV_PLAIN_FP64 if args.precision == "plain" else g.GCV_MIXED
+    use_learned = args.precision == "learned"
+    model = None
+    if use_learned:
+        from gcurval_gb300 import learned as _learned
+        model = _learned.load_model()
     batch = make_batch(args.workload, seed=rank, n_curves=args.n_curves)
     pos = batch.positions
     n_curves, n_samples = batch.n_curve, batch.total_samples
@@ -252,10 +260,13 @@ def main():
     d_out = torch.empty(n_samples, dtype=torch.float64, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
-    def device_arm(prec, steps, warmup, clocks=False):
+    def device_arm(prec, steps, warmup, clocks=False, learned_on=False):
         """Times `steps` table builds + samplings of the resident batch with CUDA
         events (L2 flushed before each); returns the per-step figures."""
-        calc = g.ArclengthCalculateGpu.from_device_batch(*d_arr, precision=prec, rtol=batch.rtol, collect_stats=True)
+        calc = g.ArclengthCalculateGpu.from_device_batch(*d_arr, precision=prec, rtol=batch.rtol, collect_stats=True,
+                                                         learned=learned_on)
+        if learned_on:
+            calc.set_learned_model(model)
 
         def step():
             calc.createArclengthTable()
@@ -266,7 +277,7 @@ def main():
         torch.cuda.synchronize()
         launches0 = calc.stats()["n_launches"]
         evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        r = {"ms_len": [], "ms_samp": [], "ms_setup": [], "n_newton": [], "n_panels": []}
+        r = {"ms_len": [], "ms_samp": [], "ms_setup": [], "n_newton": [], "n_panels": [], "ms_learned": []}
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
@@ -282,6 +293,7 @@ def main():
                 r["ms_setup"].append(st["ms_setup"] + st["ms_scan"])
                 r["n_newton"].append(st["n_newton"])
                 r["n_panels"].append(st["n_panels"])
+                r["ms_learned"].append(st["ms_learned"])
             torch.cuda.synchronize()
         if dist:
             dist.barrier()
@@ -299,10 +311,13 @@ def main():
         calc.close()
         return r
 
-    main_r = device_arm(precision, args.steps, max(args.warmup, 3), clocks=True)
-    plain_r = None
+    main_r = device_arm(precision, args.steps, max(args.warmup, 3), clocks=True, learned_on=use_learned)
+    plain_r = mixed_r = None
     if precision != g.GCV_PLAIN_FP64 and args.plain_steps > 0:
         plain_r = device_arm(g.GCV_PLAIN_FP64, args.plain_steps, 1)
+        if use_learned:
+            # the same mixed-precision walk without the network: what the network gains
+            mixed_r = device_arm(g.GCV_MIXED, args.plain_steps, 1)
     ms_per_step = main_r["ms_per_step"]
     launches = main_r["launches"]
     leaves = main_r["leaves"]
@@ -364,7 +379,9 @@ def main():
         if dist:
             dist.barrier()
         t = [time.perf_counter()]
-        c2 = g.ArclengthCalculateGpu.from_batch(batch, precision=precision, rtol=batch.rtol)
+        c2 = g.ArclengthCalculateGpu.from_batch(batch, precision=precision, rtol=batch.rtol, learned=use_learned)
+        if use_learned:
+            c2.set_learned_model(model)
         t.append(time.perf_counter())
         c2.createArclengthTable()
         t.append(time.perf_counter())
@@ -393,7 +410,7 @@ def main():
         cpu = {"value": round(sub.n_curve / secs, 3), "unit": "curves/s", "cores": nthreads, "kind": kind,
                "sample": f"{sub.n_curve} curves of the workload ({sub.total_samples} samples), table + sampling, "
                          f"{secs:.2f} s", "samples_per_s": round(sub.total_samples / secs, 1)}
-        acc = accuracy_vs_oracle(sub, precision, batch.rtol)
+        acc = accuracy_vs_oracle(sub, precision, batch.rtol, model)
     plain = None
     if plain_r is not None:
         pv = world * n_curves / (plain_r["ms_per_step"] * 1e-3)
@@ -404,12 +421,23 @@ def main():
                                "sample": round(float(np.mean(plain_r["ms_samp"])), 4),
                                "setup_scan": round(float(np.mean(plain_r["ms_setup"])), 4)},
                  "speedup_of_this_form": round(value / pv, 3)}
+    gain = None
+    if mixed_r is not None:
+        mv = world * n_curves / (mixed_r["ms_per_step"] * 1e-3)
+        gain = {"mixed_without_network": {"value": round(mv, 3), "unit": "curves/s",
+                                          "ms_per_step": round(mixed_r["ms_per_step"], 4),
+                                          "panels": float(np.mean(mixed_r["n_panels"])),
+                                          "length_ms": round(float(np.mean(mixed_r["ms_len"])), 4)},
+                "with_network": {"panels": float(np.mean(n_panels)), "length_ms": round(float(np.mean(ms_len)), 4),
+                                 "inference_ms": round(float(np.mean(main_r["ms_learned"])), 4)},
+                "panels_saved_frac": round(1.0 - float(np.mean(n_panels)) / float(np.mean(mixed_r["n_panels"])), 4),
+                "speedup_over_mixed": round(value / mv, 4)}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "curves/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == g.GCV_PLAIN_FP64 else "f32+f64",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == g.GCV_PLAIN_FP64 else ("f32+f64+bf16" if use_learned else "f32+f64"),
             "data": "synthetic: seeded generator (numpy default_rng, seed = rank)",
             "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][1]}",
                        "precision": args.precision, "rtol": batch.rtol,
@@ -425,6 +453,7 @@ def main():
             "cpu_baseline": cpu,
             "accuracy_vs_fp64_oracle": acc,
             "plain_fp64_same_batch": plain,
+            "learned_gain": gain,
             "clocks": main_r["clocks"],
         }
         print(json.dumps(line), flush=True)

@@ -139,8 +139,10 @@ class ArclengthCalculateGpu:
 
     # ---------------------------------------------------------------- makers
     @staticmethod
-    def _opts(precision=GCV_PLAIN_FP64, rtol=None, max_depth=None, stream=None, collect_stats=False) -> Options:
+    def _opts(precision=GCV_PLAIN_FP64, rtol=None, max_depth=None, stream=None, collect_stats=False,
+              learned=False) -> Options:
         o = default_options(precision)
+        o.learned = int(bool(learned))
         if rtol is not None:
             o.rtol = float(rtol)
         if max_depth is not None:
@@ -282,6 +284,27 @@ class ArclengthCalculateGpu:
         if total != n_positions:
             raise ValueError(f"sample counts add up to {total}, {n_positions} positions given")
         return total
+
+    # ------------------------------------------------------- learned form
+    def set_learned_model(self, weights):
+        """Installs the learned form's network (packed FP32 weights, see
+        gcurval_gb300.learned); None removes it.  Takes effect for contexts
+        created with learned=True."""
+        w = None if weights is None else np.ascontiguousarray(weights, np.float32)
+        if w is not None and w.size != self._lib.gcv_mlp_param_count():
+            raise ValueError(f"{w.size} weights, {self._lib.gcv_mlp_param_count()} expected")
+        check(self._lib.gcv_set_learned_model(self._h, _ptr(w)))
+
+    def learned_features(self, out):
+        """The 16 features of every knot interval into `out` (CUDA float32, n_segments x 16)."""
+        check(self._lib.gcv_learned_features(self._h, _ptr(out)))
+        return out
+
+    def learned_labels(self, depth, share, tguess):
+        """Labels from the current (plain) table into CUDA tensors: depth
+        (int32, n_segments), share (float32, n_segments x 4), tguess (float32,
+        n_segments x 8)."""
+        check(self._lib.gcv_learned_labels(self._h, _ptr(depth), _ptr(share), _ptr(tguess)))
 
     # ------------------------------------------------------------- extras
     def synchronize(self):

@@ -43,7 +43,7 @@ class GcvError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("max_depth", ctypes.c_int), ("precision", ctypes.c_int),
-                ("stream", _P), ("collect_stats", ctypes.c_int)]
+                ("stream", _P), ("collect_stats", ctypes.c_int), ("learned", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):
@@ -56,7 +56,7 @@ class Stats(ctypes.Structure):
                 ("n_panels", ctypes.c_int64), ("n_deep_segments", ctypes.c_int64), ("n_capped", ctypes.c_int64),
                 ("n_samples", ctypes.c_int64), ("n_newton", ctypes.c_int64), ("ms_setup", ctypes.c_double),
                 ("ms_length", ctypes.c_double), ("ms_scan", ctypes.c_double), ("ms_sample", ctypes.c_double),
-                ("n_launches", ctypes.c_int64)]
+                ("n_launches", ctypes.c_int64), ("ms_learned", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -89,13 +89,31 @@ _SIGS = {
     "gcv_get_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                      ctypes.POINTER(ctypes.c_int)]),
     "gcv_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "gcv_bspline_lengths_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
+                                                   ctypes.c_double, ctypes.c_int, _P, _P]),
+    # learned form (include/gcurval_gb300_learned.h)
+    "gcv_mlp_param_count": (ctypes.c_int, []),
+    "gcv_mlp_last_error": (ctypes.c_char_p, []),
+    "gcv_learned_features": (ctypes.c_int, [_P, _P]),
+    "gcv_learned_labels": (ctypes.c_int, [_P, _P, _P, _P]),
+    "gcv_mlp_trainer_create": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_ulonglong]),
+    "gcv_mlp_trainer_destroy": (ctypes.c_int, [_P]),
+    "gcv_mlp_trainer_set_weights": (ctypes.c_int, [_P, _P]),
+    "gcv_mlp_trainer_get_weights": (ctypes.c_int, [_P, _P]),
+    "gcv_mlp_trainer_forward": (ctypes.c_int, [_P, _P, ctypes.c_int, _P]),
+    "gcv_mlp_trainer_gradients": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int, _P, _P]),
+    "gcv_mlp_trainer_step": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_float, _P]),
+    "gcv_mlp_infer": (ctypes.c_int, [_P, _P, ctypes.c_int, _P]),
+    "gcv_set_learned_model": (ctypes.c_int, [_P, _P]),
 }
+
+LEARNED_HEADER = os.path.join(os.path.dirname(HEADER), "gcurval_gb300_learned.h")
 
 _lib = None
 
 
 def declared_symbols(header: str = HEADER):
-    """Names of the functions include/gcurval_gb300.h declares."""
+    """Names of the functions a header of include/ declares (default gcurval_gb300.h)."""
     import re
     txt = open(header).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)

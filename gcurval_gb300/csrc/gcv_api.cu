@@ -2,6 +2,7 @@
 // memory, and the host-side orchestration of the set-up, length, scan and
 // sampling kernels on the context's stream.
 #include "gcurval_gb300.h"
+#include "gcurval_gb300_learned.h"
 
 #include <cuda_runtime.h>
 
@@ -13,6 +14,7 @@
 #include <string>
 #include <vector>
 
+#include "gcv_learned.cuh"
 #include "gcv_length.cuh"
 #include "gcv_sample.cuh"
 #include "gcv_staging.h"
@@ -141,6 +143,9 @@ struct gcv_ctx {
     std::vector<CodeRange> code_ranges, curve_ranges;
     std::vector<int> h_curve_list;
     DBuf<int64_t> list_sample_off;  // sample-count prefix in curve_list order
+    // learned form: the network's weight image and per-interval start depths
+    void* mlp_w = nullptr;
+    DBuf<uint32_t> starts;
 
     // table
     DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_q0, seg_len, seg_cum, curve_len;
@@ -171,6 +176,7 @@ struct gcv_ctx {
     gcv_stats stats{};
     cudaEvent_t ev[8] = {};
     bool ev_table = false, ev_sample = false;
+    bool learned_ran = false;
 };
 
 namespace {
@@ -248,6 +254,8 @@ void destroy_ctx(gcv_ctx* c)
     c->seg_curve.release();
     c->seg_list.release();
     c->curve_list.release();
+    c->starts.release();
+    if (c->mlp_w) cudaFree(c->mlp_w);
     c->list_sample_off.release();
     c->coef.release();
     c->seg_t0.release();
@@ -627,6 +635,26 @@ gcv_status build_table(gcv_ctx* c)
         for (const CodeRange& r : c->code_ranges) CHECK(launch_setup_list(c, r));
     }
     CU(cudaEventRecord(c->ev[1], c->stream));
+    const bool learned = c->opt.learned && c->mlp_w && c->n_seg > 0;
+    if (learned) {
+        // start depths of every B-spline interval from the network (ellipse pieces keep 0)
+        CHECK(c->starts.reserve((size_t)c->n_seg));
+        CU(cudaMemsetAsync(c->starts.p, 0, (size_t)c->n_seg * sizeof(uint32_t), c->stream));
+        const int md = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
+        auto run = [&](const int* list, int64_t n) -> gcv_status {
+            cudaError_t e = mlp_starts_launch(b, list, n, c->mlp_w, c->opt.rtol, md, c->starts.p, c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "network inference");
+            c->stats.n_launches++;
+            return GCV_OK;
+        };
+        if (c->code > 0) {
+            CHECK(run(nullptr, c->n_seg));
+        } else if (c->code < 0) {
+            for (const CodeRange& r : c->code_ranges)
+                if (r.code != CODE_ELLIPSE) CHECK(run(c->seg_list.p + r.begin, r.end - r.begin));
+        }
+    }
+    CU(cudaEventRecord(c->ev[6], c->stream));
     for (int attempt = 0;; ++attempt) {
         if (attempt > 8) return fail(GCV_ERR_OVERFLOW, "deep list kept overflowing");
         // keep the set-up's error bits, clear the rest
@@ -643,6 +671,7 @@ gcv_status build_table(gcv_ctx* c)
         P.n_items = 0;
         P.coef_ff = c->coef_ff.p;
         P.work = c->ctr.p + C_WORK;
+        P.starts = learned ? c->starts.p : nullptr;
         if (c->n_seg > 0) CHECK(launch_main_pass(c, P));
         CHECK(read_counters(c));
         const unsigned long long err = c->h_ctr[C_ERR];
@@ -670,6 +699,7 @@ gcv_status build_table(gcv_ctx* c)
             Q.list = c->deep_list.p;
             Q.n_items = n_deep;
             Q.collect = 0;
+            Q.starts = nullptr;
             Q.work = c->ctr.p + C_WORK;
             CHECK(launch_length<1>(c, c->code, Q));
             const int rb = (int)std::min<int64_t>((n_deep + 255) / 256, (int64_t)sm_count() * 8);
@@ -709,6 +739,13 @@ gcv_status build_table(gcv_ctx* c)
     }
     CU(cudaEventRecord(c->ev[3], c->stream));
     c->ev_table = true;
+    if (learned) {
+        unsigned err = 0;
+        CU(cudaMemcpyAsync(&err, (uint8_t*)c->mlp_w + mlp_dev_bytes(), sizeof(err), cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+        if (err) return fail(GCV_ERR_TIMEOUT, "network inference: a tensor-core wait gave up");
+    }
+    c->learned_ran = learned;
     return GCV_OK;
 }
 
@@ -1246,6 +1283,9 @@ gcv_status gcv_get_stats(gcv_ctx* ctx, gcv_stats* out)
     if (ctx->ev_table) {
         if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]) == cudaSuccess) ctx->stats.ms_setup = ms;
         if (cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]) == cudaSuccess) ctx->stats.ms_length = ms;
+        ctx->stats.ms_learned = 0.0;
+        if (ctx->learned_ran && cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[6]) == cudaSuccess)
+            ctx->stats.ms_learned = ms;
         if (cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]) == cudaSuccess) ctx->stats.ms_scan = ms;
     }
     if (ctx->ev_sample) {
@@ -1303,6 +1343,54 @@ gcv_status gcv_get_shape(gcv_ctx* ctx, int64_t* n_curve, int64_t* n_segments, in
     if (n_curve) *n_curve = ctx->n_curve;
     if (n_segments) *n_segments = ctx->n_seg;
     if (point_dim) *point_dim = ctx->point_dim;
+    return GCV_OK;
+}
+
+gcv_status gcv_learned_features(gcv_ctx* ctx, float* d_features)
+{
+    if (!ctx || (!d_features && ctx->n_seg > 0)) return fail(GCV_ERR_INVALID, "NULL argument");
+    if (ctx->n_seg == 0) return GCV_OK;
+    const int blocks = (int)std::min<int64_t>((ctx->n_seg + 255) / 256, (int64_t)sm_count() * 32);
+    k_features<<<blocks, 256, 0, ctx->stream>>>(batch_view(ctx), ctx->opt.rtol, d_features);
+    CU(cudaGetLastError());
+    ctx->stats.n_launches++;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return GCV_OK;
+}
+
+gcv_status gcv_learned_labels(gcv_ctx* ctx, int* d_depth, float* d_share, float* d_tguess)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    if (!ctx->table_ready) return fail(GCV_ERR_STATE, "createArclengthTable has not run");
+    if (ctx->learned_ran) return fail(GCV_ERR_STATE, "labels come from a table built by the plain walk");
+    if (ctx->n_seg == 0) return GCV_OK;
+    if (!d_depth || !d_share || !d_tguess) return fail(GCV_ERR_INVALID, "NULL label array");
+    const int blocks = (int)std::min<int64_t>((ctx->n_seg + 255) / 256, (int64_t)sm_count() * 32);
+    k_labels<<<blocks, 256, 0, ctx->stream>>>(table_view(ctx), ctx->n_seg, d_depth, d_share, d_tguess);
+    CU(cudaGetLastError());
+    ctx->stats.n_launches++;
+    CU(cudaStreamSynchronize(ctx->stream));
+    return GCV_OK;
+}
+
+gcv_status gcv_set_learned_model(gcv_ctx* ctx, const float* host_weights)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (ctx->mlp_w) {
+        cudaFree(ctx->mlp_w);
+        ctx->mlp_w = nullptr;
+    }
+    if (!host_weights) return GCV_OK;
+    for (int i = 0; i < MLP_NPARAM; ++i)
+        if (!std::isfinite(host_weights[i])) return fail(GCV_ERR_INVALID, "network weights hold NaN or infinity");
+    void* w = nullptr;
+    cudaError_t e = mlp_upload_bf16(host_weights, &w);
+    if (e != cudaSuccess) {
+        if (w) cudaFree(w);
+        return cuda_fail(e, "network upload");
+    }
+    ctx->mlp_w = w;
     return GCV_OK;
 }
 

@@ -43,6 +43,7 @@ struct LengthParams {
     int64_t n_items;
     const float2* coef_ff;  // float-float copy of the coefficients (PREC 1)
     unsigned long long* work;  // work-queue head of this launch (starts at 0)
+    const uint32_t* starts;    // learned quarter start depths per segment (NULL: plain walk)
 };
 
 // Launches k_length<MODE, CODE, PREC> over P (persistent grid sized from the

@@ -2,7 +2,10 @@
 // included only by the gcv_len_*.cu units that instantiate them.
 #pragma once
 
+#include <type_traits>
+
 #include "gcv_ff_eval.cuh"
+#include "gcv_learned.cuh"
 #include "gcv_length.cuh"
 
 namespace gcv {
@@ -50,6 +53,30 @@ __device__ __forceinline__ int warp_incl_scan(int x, int lane)
     return x;
 }
 
+// |C(1) - C(-1)| of a B-spline piece from its derivative polynomial
+// b_m = (m + 1) a_{m+1}: C(1) - C(-1) = 2 sum_{m even} b_m / (m + 1).  A lower
+// bound of the piece's length, so rtol * chord is a tolerance no looser than
+// the plain walk's rtol * |K15 of the whole interval|.
+template <int CODE, typename T>
+__device__ __forceinline__ float chord_of(const T* r)
+{
+    constexpr int Pd = code_degree(CODE), D = code_dim(CODE);
+    float c2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int m = 0; m < Pd; m += 2) {
+            if constexpr (std::is_same<T, ff>::value)
+                acc += r[m * D + d].hi / (float)(m + 1);
+            else
+                acc += (float)r[m * D + d] / (float)(m + 1);
+        }
+        c2 += 4.0f * acc * acc;
+    }
+    return sqrtf(c2);
+}
+
 // PREC 0: FP64 panels; PREC 1: float-float panels (GCV_MIXED), whose K15 /
 // G7 / end values enter the same FP64 bookkeeping (error test, leaf table).
 template <int MODE, int CODE, int PREC = 0>
@@ -80,6 +107,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
     double cum = 0.0, tol_unit = 0.0;
     ff cumf{0.0f, 0.0f};  // float-float running sum (PREC 1)
     float tol_f = 0.0f;
+    uint32_t dq = 0;  // learned quarter start depths of the segment (0: plain walk)
     long long panels = 0;
     unsigned long long my_panels = 0, my_capped = 0, my_nonfinite = 0;
 
@@ -119,6 +147,24 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                     cum = 0.0;
                     cumf = ff{0.0f, 0.0f};
                     panels = 0;
+                    dq = 0;
+                    if constexpr (MODE == 0 && CODE > 0) {
+                        // learned start: the predicted depths, tolerance from the chord
+                        if (P.starts) {
+                            const uint32_t q = P.starts[s];
+                            float ch;
+                            if constexpr (PREC == 1)
+                                ch = chord_of<CODE>(rf);
+                            else
+                                ch = chord_of<CODE>(r);
+                            if (q != 0u && ch > 0.0f) {
+                                dq = q;
+                                tol_unit = P.rtol * (double)ch;
+                                tol_f = (float)tol_unit;
+                                learned_descend(dq, k, depth);
+                            }
+                        }
+                    }
                     if (MODE == 2) {
                         pool = (int64_t)atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)t.leaf_cnt[s]);
                         if (pool + t.leaf_cnt[s] > t.leaf_cap) {
@@ -226,6 +272,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                 const int tz = __ffsll((long long)k) - 1;
                 k >>= tz;
                 depth -= tz;
+                if (dq && depth > 0) learned_descend(dq, k, depth);
                 if (ovf) {
                     active = false;
                 } else if (depth == 0) {

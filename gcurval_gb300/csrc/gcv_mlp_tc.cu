@@ -1,0 +1,396 @@
+// BF16 tensor-core inference of the learned form's MLP (tcgen05, sm_103a).
+//
+// One CTA = two warpgroups; each warpgroup runs its own tiles of 128
+// intervals (M = 128 rows, one row per thread and TMEM lane):
+//   features (computed in the kernel, or read) -> bf16 tile X [128 x 16]
+//   D = X W1        1 x tcgen05.mma (K = 16), D in TMEM (128 lanes x 128 cols, FP32)
+//   H1 = GELU(D + b1) -> bf16 tile [128 x 128] in shared memory
+//   D = H1 W2, H2, D = H2 W3, H3: 8 MMAs each (K = 128 in steps of 16)
+//   D = H3 W4 (N = 32): outputs -> start depths of the length walk (or raw)
+// The transposed weights W^T (N x K) stay in shared memory for the whole
+// kernel; operands use the no-swizzle K-major core-matrix layout (8 rows x
+// 16 bytes per core matrix; LBO = 128 B between core matrices along K,
+// SBO between 8-row groups).  One thread per warpgroup issues the MMAs and
+// commits them to the warpgroup's mbarrier; every wait is bounded and a
+// timeout is reported through an error word, after which the kernel still
+// releases its tensor memory.
+#include "gcurval_gb300_learned.h"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gcv_learned.cuh"
+
+namespace gcv {
+
+namespace {
+
+// byte offsets of the weight image (identical in global and shared memory)
+constexpr int WB_W4 = 0;                                // W4^T [32][128]
+constexpr int WB_W1 = WB_W4 + MLP_OUT * MLP_H * 2;      // W1^T [128][16]
+constexpr int WB_W2 = WB_W1 + MLP_H * MLP_IN * 2;       // W2^T [128][128]
+constexpr int WB_W3 = WB_W2 + MLP_H * MLP_H * 2;        // W3^T [128][128]
+constexpr int WB_BIAS = WB_W3 + MLP_H * MLP_H * 2;      // b1, b2, b3 (128 each), b4 (32), FP32
+constexpr int WB_BYTES = WB_BIAS + (3 * MLP_H + MLP_OUT) * 4;
+constexpr int SM_X = (WB_BYTES + 127) / 128 * 128;      // two X tiles [128][16] bf16
+constexpr int X_BYTES = 128 * MLP_IN * 2;
+constexpr int SM_A = SM_X + 2 * X_BYTES;                // two H tiles [128][128] bf16
+constexpr int A_BYTES = 128 * MLP_H * 2;
+constexpr int SM_BAR = SM_A + 2 * A_BYTES;              // two mbarriers, the TMEM address
+constexpr int SM_BYTES = SM_BAR + 32;
+constexpr int TC_THREADS = 256;
+constexpr int TMEM_COLS = 256;                          // 128 FP32 columns per warpgroup
+constexpr long long WAIT_LIMIT = 1ll << 24;
+
+// canonical no-swizzle K-major offset of element (row, k) in a tile with K columns
+__host__ __device__ constexpr int kmaj_off(int row, int k, int K)
+{
+    return (row >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start, LBO, SBO (bytes, >> 4), version 1, no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::f16: D F32, A and B BF16, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (long long i = 0; i < WAIT_LIMIT; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void wg_sync(int wg) { asm volatile("bar.sync %0, 128;" ::"r"(1 + wg) : "memory"); }
+// barrier of the warpgroup that also ANDs a flag over its 128 threads
+__device__ __forceinline__ bool wg_all(int wg, bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.and.pred q, %2, 128, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "r"(1 + wg)
+        : "memory");
+    return r != 0;
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float gelu_fast(float x)
+{
+    float t;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(GELU_C * (x + GELU_A * x * x * x)));
+    return 0.5f * x * (1.0f + t);
+}
+
+// 8 values -> 8 bf16 at a 16-byte aligned shared address
+__device__ __forceinline__ void st_bf16x8(uint8_t* p, const float* v)
+{
+    __nv_bfloat162 h[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(v[2 * i], v[2 * i + 1]);
+    *reinterpret_cast<uint4*>(p) = *reinterpret_cast<const uint4*>(h);
+}
+
+struct TcArgs {
+    // product path: features from the batch, start depths out
+    Batch b;
+    const int* list;
+    double rtol;
+    int max_depth;
+    uint32_t* starts;
+    // test path: features in, raw outputs out
+    const float* feat;
+    float* out;
+    int64_t n;
+    const uint8_t* w;  // weight image (WB_BYTES)
+    unsigned* err;
+};
+
+template <bool FROM_BATCH>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
+{
+    extern __shared__ __align__(1024) uint8_t sm[];
+    const int tid = threadIdx.x, wg = tid >> 7, t = tid & 127, warp = tid >> 5;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + SM_BAR);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SM_BAR + 16);
+    const float* bias = reinterpret_cast<const float*>(sm + WB_BIAS);
+
+    // weights into shared memory
+    for (int i = tid; i < WB_BYTES / 16; i += TC_THREADS)
+        reinterpret_cast<uint4*>(sm)[i] = reinterpret_cast<const uint4*>(A.w)[i];
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t tcol = tmem + 128u * wg;                         // this warpgroup's columns
+    const uint32_t tlane = tcol + ((uint32_t)(32 * (warp & 3)) << 16);  // this warp's lanes
+    uint8_t* X = sm + SM_X + wg * X_BYTES;
+    uint8_t* H = sm + SM_A + wg * A_BYTES;
+    const uint32_t bar = smem_u32(&bars[wg]);
+    uint32_t parity = 0;
+    bool ok = true;
+
+    const int64_t tiles = (A.n + 127) / 128;
+    for (int64_t tile = (int64_t)blockIdx.x * 2 + wg; tile < tiles && ok; tile += (int64_t)gridDim.x * 2) {
+        const int64_t row = tile * 128 + t;
+        const bool live = row < A.n;
+        int64_t s = row;
+        // ---- features -> X (bf16, K-major core matrices, K = 16)
+        float f[MLP_IN];
+        if constexpr (FROM_BATCH) {
+            if (live) {
+                s = A.list ? (int64_t)A.list[row] : row;
+                interval_features(A.b, s, A.rtol, f);
+            } else {
+#pragma unroll
+                for (int i = 0; i < MLP_IN; ++i) f[i] = 0.0f;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < MLP_IN; ++i) f[i] = live ? A.feat[row * MLP_IN + i] : 0.0f;
+        }
+        st_bf16x8(X + kmaj_off(t, 0, MLP_IN), f);
+        st_bf16x8(X + kmaj_off(t, 8, MLP_IN), f + 8);
+        fence_async_smem();
+        fence_before();
+        wg_sync(wg);
+        fence_after();
+        // ---- four layers
+        for (int layer = 0; layer < 4 && ok; ++layer) {
+            const int N = layer == 3 ? MLP_OUT : MLP_H;
+            if (t == 0) {
+                const uint32_t idesc = idesc_bf16(128, N);
+                const uint32_t wbase = smem_u32(sm) + (layer == 0 ? WB_W1 : layer == 1 ? WB_W2 : layer == 2 ? WB_W3 : WB_W4);
+                if (layer == 0) {
+                    mma_bf16(tcol, sdesc(smem_u32(X), 128, (MLP_IN / 8) * 128), sdesc(wbase, 128, (MLP_IN / 8) * 128),
+                             idesc, 0u);
+                } else {
+#pragma unroll 1
+                    for (int ks = 0; ks < MLP_H / 16; ++ks)  // K steps of 16 = two core matrices
+                        mma_bf16(tcol, sdesc(smem_u32(H) + ks * 256, 128, (MLP_H / 8) * 128),
+                                 sdesc(wbase + ks * 256, 128, (MLP_H / 8) * 128), idesc, ks > 0 ? 1u : 0u);
+                }
+                mma_commit(bar);
+            }
+            ok = wg_all(wg, mbar_wait(bar, parity));  // uniform over the warpgroup
+            parity ^= 1u;
+            fence_after();
+            if (!ok) break;
+            if (layer < 3) {
+                // epilogue: bias + GELU -> bf16 H (the MMAs reading H have completed)
+                const float* bl = bias + layer * MLP_H;
+#pragma unroll 1
+                for (int c = 0; c < MLP_H / 32; ++c) {
+                    float v[32];
+                    tmem_ld32(tlane + 32u * c, v);
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) v[i] = gelu_fast(v[i] + bl[32 * c + i]);
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) st_bf16x8(H + kmaj_off(t, 32 * c + 8 * q, MLP_H), v + 8 * q);
+                }
+                fence_async_smem();
+                fence_before();
+                wg_sync(wg);
+                fence_after();
+            } else {
+                float o[32];
+                tmem_ld32(tlane, o);
+                const float* bl = bias + 3 * MLP_H;
+#pragma unroll
+                for (int i = 0; i < 32; ++i) o[i] += bl[i];
+                if (live) {
+                    if constexpr (FROM_BATCH) {
+                        // ellipse pieces and empty intervals keep the plain start
+                        const int64_t c = A.b.seg_curve[s];
+                        A.starts[s] = A.b.kind[c] == 0 ? 0u : quarter_depths(o, A.max_depth);
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < 32; ++i) A.out[row * MLP_OUT + i] = o[i];
+                    }
+                }
+                // TMEM columns are reused by the next tile's first MMA
+                fence_before();
+                wg_sync(wg);
+                fence_after();
+            }
+        }
+    }
+    if (!ok && t == 0) atomicOr(A.err, 1u);
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+int sm_count_tc()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <bool FROM_BATCH>
+cudaError_t launch_tc(const TcArgs& A, cudaStream_t stream)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc<FROM_BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES);
+    if (e != cudaSuccess) return e;
+    const int64_t tiles = (A.n + 127) / 128;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tiles + 1) / 2, sm_count_tc()));
+    k_mlp_tc<FROM_BATCH><<<grid, TC_THREADS, SM_BYTES, stream>>>(A);
+    return cudaGetLastError();
+}
+
+// host: packed FP32 weights -> the bf16 weight image
+std::vector<uint8_t> weight_image(const float* w)
+{
+    std::vector<uint8_t> img(WB_BYTES, 0);
+    auto put = [&](int base, int N, int K, int off) {  // W[k][n] (K x N) -> W^T core-matrix tile
+        for (int n = 0; n < N; ++n)
+            for (int k = 0; k < K; ++k) {
+                const __nv_bfloat16 h = __float2bfloat16_rn(w[off + k * N + n]);
+                std::memcpy(&img[(size_t)base + kmaj_off(n, k, K)], &h, 2);
+            }
+    };
+    put(WB_W1, MLP_H, MLP_IN, MLP_OFF_W1);
+    put(WB_W2, MLP_H, MLP_H, MLP_OFF_W2);
+    put(WB_W3, MLP_H, MLP_H, MLP_OFF_W3);
+    put(WB_W4, MLP_OUT, MLP_H, MLP_OFF_W4);
+    float* b = reinterpret_cast<float*>(&img[WB_BIAS]);
+    std::memcpy(b, w + MLP_OFF_B1, MLP_H * 4);
+    std::memcpy(b + MLP_H, w + MLP_OFF_B2, MLP_H * 4);
+    std::memcpy(b + 2 * MLP_H, w + MLP_OFF_B3, MLP_H * 4);
+    std::memcpy(b + 3 * MLP_H, w + MLP_OFF_B4, MLP_OUT * 4);
+    return img;
+}
+
+}  // namespace
+
+size_t mlp_dev_bytes() { return WB_BYTES; }
+
+cudaError_t mlp_upload_bf16(const float* host_w, void** w_dev)
+{
+    const std::vector<uint8_t> img = weight_image(host_w);
+    cudaError_t e = cudaMalloc(w_dev, WB_BYTES + sizeof(unsigned));
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(*w_dev, img.data(), WB_BYTES, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset((uint8_t*)*w_dev + WB_BYTES, 0, sizeof(unsigned));
+    return e;
+}
+
+cudaError_t mlp_starts_launch(const Batch& b, const int* list, int64_t n, const void* w_dev, double rtol, int max_depth,
+                              uint32_t* starts, cudaStream_t stream)
+{
+    if (n <= 0) return cudaSuccess;
+    TcArgs A{};
+    A.b = b;
+    A.list = list;
+    A.rtol = rtol;
+    A.max_depth = max_depth;
+    A.starts = starts;
+    A.n = n;
+    A.w = (const uint8_t*)w_dev;
+    A.err = (unsigned*)((uint8_t*)w_dev + WB_BYTES);
+    return launch_tc<true>(A, stream);
+}
+
+}  // namespace gcv
+
+extern "C" gcv_status gcv_mlp_infer(const float* host_weights, const float* d_features, int n, float* d_out)
+{
+    using namespace gcv;
+    if (!host_weights || (n > 0 && (!d_features || !d_out)) || n < 0) return GCV_ERR_INVALID;
+    if (n == 0) return GCV_OK;
+    void* w = nullptr;
+    cudaError_t e = mlp_upload_bf16(host_weights, &w);
+    if (e == cudaSuccess) {
+        TcArgs A{};
+        A.feat = d_features;
+        A.out = d_out;
+        A.n = n;
+        A.w = (const uint8_t*)w;
+        A.err = (unsigned*)((uint8_t*)w + WB_BYTES);
+        e = launch_tc<false>(A, nullptr);
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
+    unsigned err = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&err, (uint8_t*)w + WB_BYTES, sizeof(err), cudaMemcpyDeviceToHost);
+    if (w) cudaFree(w);
+    if (e != cudaSuccess) return GCV_ERR_CUDA;
+    return err ? GCV_ERR_TIMEOUT : GCV_OK;
+}

@@ -6,6 +6,7 @@
 
 #include "gcv_ff_eval.cuh"
 #include "gcv_kernels.cuh"
+#include "gcv_learned.cuh"
 
 namespace gcv {
 
@@ -255,6 +256,65 @@ static __global__ void k_curve_len(Batch b, Table t)
          c += (int64_t)gridDim.x * blockDim.x) {
         const int64_t e = b.seg_off[c + 1];
         t.curve_len[c] = e > b.seg_off[c] ? t.seg_cum[e - 1] : 0.0;
+    }
+}
+
+// ------------------------------------------------- learned form: data
+// features of every interval (16 floats each)
+static __global__ void k_features(Batch b, double rtol, float* __restrict__ out)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < b.n_seg; s += (int64_t)gridDim.x * blockDim.x) {
+        float f[MLP_IN];
+        interval_features(b, s, rtol, f);
+#pragma unroll
+        for (int i = 0; i < MLP_IN; ++i) out[s * MLP_IN + i] = f[i];
+    }
+}
+
+// labels from a plain table: shallowest leaf depth (capped), leaf share per
+// quarter, and the local parameter at arc-length fractions (j + 1/2) / 8 by
+// cubic Hermite interpolation of v(S) on the leaf (v' = 1 / f at its ends)
+static __global__ void k_labels(Table t, int64_t n_seg, int* __restrict__ depth, float* __restrict__ share,
+                                float* __restrict__ tg)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n_seg; s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t off = t.leaf_off[s];
+        const int cnt = t.leaf_cnt[s];
+        const double len = t.seg_len[s];
+        if (!(t.seg_t1[s] > t.seg_t0[s]) || cnt <= 0 || !(len > 0.0)) {
+            depth[s] = 0;
+            for (int q = 0; q < 4; ++q) share[s * 4 + q] = 0.25f;
+            for (int j = 0; j < 8; ++j) tg[s * 8 + j] = -1.0f + (2.0f * j + 1.0f) / 8.0f;
+            continue;
+        }
+        int dmin = 64, qc[4] = {0, 0, 0, 0};
+        double va = -1.0;
+        for (int j = 0; j < cnt; ++j) {
+            const double vb = t.leaf_v[off + j];
+            const int d = 1 - ilogb(vb - va);  // width 2^(1 - d)
+            dmin = min(dmin, d);
+            qc[min(3, max(0, (int)((0.5 * (va + vb) + 1.0) * 2.0)))]++;
+            va = vb;
+        }
+        depth[s] = min(dmin, MLP_MAX_DEPTH);
+        for (int q = 0; q < 4; ++q) share[s * 4 + q] = (float)qc[q] / (float)cnt;
+        int j = 0;
+        for (int k8 = 0; k8 < 8; ++k8) {
+            const double target = (k8 + 0.5) / 8.0 * len;
+            while (j < cnt - 1 && t.leaf_cum[off + j] < target) ++j;
+            const double base = j ? t.leaf_cum[off + j - 1] : 0.0, cb = t.leaf_cum[off + j];
+            const double a = j ? t.leaf_v[off + j - 1] : -1.0, bv = t.leaf_v[off + j];
+            const double fa = j ? (double)t.leaf_f[off + j - 1] : t.seg_f0[s], fb = (double)t.leaf_f[off + j];
+            const double dS = cb - base;
+            const double sg = dS > 0.0 ? fmin(fmax((target - base) / dS, 0.0), 1.0) : 0.0;
+            double v = a + sg * (bv - a);
+            if (fa > 0.0 && fb > 0.0) {
+                const double s2 = sg * sg, s3 = s2 * sg;
+                v = (2 * s3 - 3 * s2 + 1) * a + (-2 * s3 + 3 * s2) * bv + dS * ((s3 - 2 * s2 + sg) / fa + (s3 - s2) / fb);
+                v = fmin(fmax(v, a), bv);
+            }
+            tg[s * 8 + k8] = (float)v;
+        }
     }
 }
 

@@ -75,6 +75,9 @@ typedef struct gcv_options {
     int precision;        /* gcv_precision */
     void* stream;         /* cudaStream_t; NULL = legacy default stream */
     int collect_stats;    /* nonzero: count panels and Newton steps (gcv_get_stats) */
+    int learned;          /* nonzero: start B-spline intervals at the depths predicted by the
+                             network installed with gcv_set_learned_model
+                             (gcurval_gb300_learned.h); no effect without one */
 } gcv_options;
 
 typedef struct gcv_ctx gcv_ctx;
@@ -106,6 +109,7 @@ typedef struct gcv_stats {
     int64_t n_newton;         /* Newton iterations of the sampling kernel */
     double ms_setup, ms_length, ms_scan, ms_sample;  /* device time per phase */
     int64_t n_launches;       /* kernels launched by the context so far */
+    double ms_learned;        /* network inference inside ms_length (learned form) */
 } gcv_stats;
 
 const char* gcv_status_string(gcv_status s);
