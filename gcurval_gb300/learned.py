@@ -25,7 +25,7 @@ import numpy as np
 from . import _lib
 from ._lib import GCV_PLAIN_FP64, check
 
-MODEL_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "mlp_uneven_rtol1e-8.npz")
+MODEL_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "mlp_uneven.npz")
 N_PARAM = 39328  # gcv_mlp_param_count()
 
 
@@ -48,7 +48,7 @@ def load_model(path: str = MODEL_PATH) -> np.ndarray:
     return w
 
 
-def training_set(n_intervals: int, seed: int, rtol: float = 1e-8, chunk_curves: int = 4000):
+def training_set(n_intervals: int, seed: int, rtol: float = 5e-9, chunk_curves: int = 4000):
     """(X, depth, share, tguess) CUDA tensors of n_intervals B-spline knot
     intervals of positive width, labelled by the plain FP64 walk at rtol."""
     import torch
@@ -190,7 +190,7 @@ def main(argv=None):
     ap.add_argument("--train", action="store_true")
     ap.add_argument("--intervals", type=int, default=5_000_000)
     ap.add_argument("--epochs", type=int, default=6)
-    ap.add_argument("--rtol", type=float, default=1e-8)
+    ap.add_argument("--rtol", type=float, default=5e-9, help="the uneven batch's per-interval tolerance")
     ap.add_argument("--out", default=MODEL_PATH)
     a = ap.parse_args(argv)
     if not a.train:

@@ -72,7 +72,7 @@ def test_tensor_core_inference_matches_fp32(gpu_lib, n):
 
 def test_short_training_reduces_the_loss(gpu_lib):
     b = ds.uneven_batch(300, seed=21)
-    calc = g.ArclengthCalculateGpu.from_batch(b, precision=g.GCV_PLAIN_FP64, rtol=1e-8)
+    calc = g.ArclengthCalculateGpu.from_batch(b, precision=g.GCV_PLAIN_FP64, rtol=b.rtol)
     calc.createArclengthTable()
     n = calc.n_segments
     X = torch.empty((n, 16), dtype=torch.float32, device="cuda")
@@ -97,7 +97,7 @@ def test_short_training_reduces_the_loss(gpu_lib):
 
 
 def _table(b, learned_on, w=None):
-    calc = g.ArclengthCalculateGpu.from_batch(b, precision=g.GCV_MIXED, rtol=1e-8, collect_stats=True,
+    calc = g.ArclengthCalculateGpu.from_batch(b, precision=g.GCV_MIXED, rtol=b.rtol, collect_stats=True,
                                              learned=learned_on)
     if w is not None:
         calc.set_learned_model(w)
