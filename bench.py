@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="uneven_batch")
-    ap.add_argument("--precision", choices=["plain", "mixed", "learned"], default="mixed",
+    ap.add_argument("--precision", choices=["plain", "mixed", "learned"], default="learned",
                     help="plain FP64, mixed precision, or mixed precision with the learned start depths")
     ap.add_argument("--plain-steps", type=int, default=3,
                     help="timed steps of the plain FP64 form on the same batch, for the speed-up (0: skip)")

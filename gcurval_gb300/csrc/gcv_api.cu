@@ -113,6 +113,7 @@ int sm_count()
 
 }  // namespace
 
+constexpr int64_t LEARNED_CHUNK = 1 << 24;  // intervals per feature chunk of the learned form (1 GiB)
 constexpr int STREAM_EVENTS = 4;  // host-buffer sampling: events per stage, used round robin
 
 struct CodeRange {
@@ -146,6 +147,7 @@ struct gcv_ctx {
     // learned form: the network's weight image and per-interval start depths
     void* mlp_w = nullptr;
     DBuf<uint32_t> starts;
+    DBuf<float> feat;  // features of one chunk of intervals
 
     // table
     DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_q0, seg_len, seg_cum, curve_len;
@@ -255,6 +257,7 @@ void destroy_ctx(gcv_ctx* c)
     c->seg_list.release();
     c->curve_list.release();
     c->starts.release();
+    c->feat.release();
     if (c->mlp_w) cudaFree(c->mlp_w);
     c->list_sample_off.release();
     c->coef.release();
@@ -641,8 +644,11 @@ gcv_status build_table(gcv_ctx* c)
         CHECK(c->starts.reserve((size_t)c->n_seg));
         CU(cudaMemsetAsync(c->starts.p, 0, (size_t)c->n_seg * sizeof(uint32_t), c->stream));
         const int md = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
+        const int64_t rows = std::min<int64_t>(c->n_seg, LEARNED_CHUNK);
+        CHECK(c->feat.reserve((size_t)rows * MLP_IN));
         auto run = [&](const int* list, int64_t n) -> gcv_status {
-            cudaError_t e = mlp_starts_launch(b, list, n, c->mlp_w, c->opt.rtol, md, c->starts.p, c->stream);
+            cudaError_t e = mlp_starts_launch(b, list, n, c->mlp_w, c->opt.rtol, md, c->starts.p, c->feat.p, rows,
+                                              c->stream);
             if (e != cudaSuccess) return cuda_fail(e, "network inference");
             c->stats.n_launches++;
             return GCV_OK;
@@ -1351,7 +1357,7 @@ gcv_status gcv_learned_features(gcv_ctx* ctx, float* d_features)
     if (!ctx || (!d_features && ctx->n_seg > 0)) return fail(GCV_ERR_INVALID, "NULL argument");
     if (ctx->n_seg == 0) return GCV_OK;
     const int blocks = (int)std::min<int64_t>((ctx->n_seg + 255) / 256, (int64_t)sm_count() * 32);
-    k_features<<<blocks, 256, 0, ctx->stream>>>(batch_view(ctx), ctx->opt.rtol, d_features);
+    k_features<<<blocks, 256, 0, ctx->stream>>>(batch_view(ctx), rtol_feature(ctx->opt.rtol), d_features);
     CU(cudaGetLastError());
     ctx->stats.n_launches++;
     CU(cudaStreamSynchronize(ctx->stream));

@@ -11,6 +11,8 @@
 // the start-depth rule shared by the kernels.
 #pragma once
 
+#include <cmath>
+
 #include "gcv_table.cuh"
 
 namespace gcv {
@@ -49,7 +51,8 @@ constexpr float GELU_A = 0.044715f;
 //        to [-8, 8], / 8,
 //   14 log2(polygon length / chord) clamped to [0, 8], / 4,
 //   15 -log10(rtol) / 10.
-__device__ inline void interval_features(const Batch& b, int64_t s, double rtol, float* f)
+// Computed in FP32 apart from the knot and control-point differences.
+__device__ inline void interval_features(const Batch& b, int64_t s, float log_rtol_feature, float* f)
 {
 #pragma unroll
     for (int i = 0; i < MLP_IN; ++i) f[i] = 0.0f;
@@ -60,11 +63,13 @@ __device__ inline void interval_features(const Batch& b, int64_t s, double rtol,
     const double* kv = b.knots + b.knot_off[c];
     const double* cp = b.ctrl + b.ctrl_off[c];
     const int span = int(j) + p;
-    const double w = kv[span + 1] - kv[span];
+    // knot differences in FP64 (near-duplicate knots), the rest in FP32
+    const double k0 = kv[span];
+    const float w = (float)(kv[span + 1] - k0);
     f[0] = p * 0.2f;
     f[1] = (float)(D - 2);
-    f[15] = (float)(-log10(rtol) * 0.1);
-    if (!(w > 0.0)) return;
+    f[15] = log_rtol_feature;
+    if (!(w > 0.0f)) return;
     // control polygon of the interval, relative to its first point
     float q[6][3];
     for (int i = 0; i <= p; ++i)
@@ -78,7 +83,8 @@ __device__ inline void interval_features(const Batch& b, int64_t s, double rtol,
     }
     for (int i = 0; i < 4; ++i) f[7 + i] = 1.0f;
     if (sum > 0.0f) {
-        for (int i = 0; i < p; ++i) f[2 + i] = e[i] / sum;
+        const float inv = 1.0f / sum;
+        for (int i = 0; i < p; ++i) f[2 + i] = e[i] * inv;
         for (int i = 0; i + 1 < p; ++i) {
             float dot = 0.0f;
             for (int d = 0; d < 3; ++d) dot += (q[i + 1][d] - q[i][d]) * (q[i + 2][d] - q[i + 1][d]);
@@ -87,14 +93,17 @@ __device__ inline void interval_features(const Batch& b, int64_t s, double rtol,
         }
         const float cx = q[p][0], cy = q[p][1], cz = q[p][2];
         const float chord = sqrtf(cx * cx + cy * cy + cz * cz);
-        f[14] = chord > 0.0f ? fminf(fmaxf(log2f(sum / chord), 0.0f), 8.0f) * 0.25f : 2.0f;
+        f[14] = chord > 0.0f ? fminf(fmaxf(__log2f(sum / chord), 0.0f), 8.0f) * 0.25f : 2.0f;
     }
-    const double support = kv[span + p + 1] - kv[span - p];
-    f[11] = support > 0.0 ? (float)(w / support) : 0.0f;
-    const double wl = kv[span] - kv[span - 1], wr = kv[span + 2] - kv[span + 1];
-    f[12] = wl > 0.0 ? fminf(fmaxf((float)log2(wl / w), -8.0f), 8.0f) * 0.125f : -1.0f;
-    f[13] = wr > 0.0 ? fminf(fmaxf((float)log2(wr / w), -8.0f), 8.0f) * 0.125f : -1.0f;
+    const float support = (float)(kv[span + p + 1] - kv[span - p]);
+    f[11] = support > 0.0f ? w / support : 0.0f;
+    const float wl = (float)(k0 - kv[span - 1]), wr = (float)(kv[span + 2] - kv[span + 1]);
+    f[12] = wl > 0.0f ? fminf(fmaxf(__log2f(wl / w), -8.0f), 8.0f) * 0.125f : -1.0f;
+    f[13] = wr > 0.0f ? fminf(fmaxf(__log2f(wr / w), -8.0f), 8.0f) * 0.125f : -1.0f;
 }
+
+// feature 15: -log10(rtol) / 10
+inline float rtol_feature(double rtol) { return (float)(-std::log10(rtol) * 0.1); }
 
 // Start depth of the learned walk for the node (k, depth): the quarter
 // depths dq (one byte each) of the quarters the node covers (their minimum
@@ -146,12 +155,12 @@ __device__ __forceinline__ uint32_t quarter_depths(const float* o, int max_depth
     return out;
 }
 
-// tcgen05 MLP over the intervals of `list` (NULL: 0 .. n - 1) with features
-// computed in the kernel: quarter start depths per interval into starts[s]
-// (defined in gcv_mlp_tc.cu).  w_bf16: the device copy made by
-// mlp_upload_bf16.
+// Start depths of the intervals list[0 .. n) (list NULL: 0 .. n - 1) into
+// starts[s]: in chunks of feat_rows intervals, their features into `feat`
+// (feat_rows x 16 floats), then the tcgen05 network over the chunk (defined
+// in gcv_mlp_tc.cu).  w_dev: the device copy made by mlp_upload_bf16.
 cudaError_t mlp_starts_launch(const Batch& b, const int* list, int64_t n, const void* w_dev, double rtol,
-                              int max_depth, uint32_t* starts, cudaStream_t stream);
+                              int max_depth, uint32_t* starts, float* feat, int64_t feat_rows, cudaStream_t stream);
 // device copy of the packed FP32 weights in the inference kernel's layout
 cudaError_t mlp_upload_bf16(const float* host_w, void** w_dev);
 size_t mlp_dev_bytes();

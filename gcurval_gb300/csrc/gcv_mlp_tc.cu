@@ -1,8 +1,8 @@
 // BF16 tensor-core inference of the learned form's MLP (tcgen05, sm_103a).
 //
-// One CTA = two warpgroups; each warpgroup runs its own tiles of 128
+// One CTA = four warpgroups; each warpgroup runs its own tiles of 128
 // intervals (M = 128 rows, one row per thread and TMEM lane):
-//   features (computed in the kernel, or read) -> bf16 tile X [128 x 16]
+//   features (FP32 rows, written by k_feature_rows) -> bf16 tile X [128 x 16]
 //   D = X W1        1 x tcgen05.mma (K = 16), D in TMEM (128 lanes x 128 cols, FP32)
 //   H1 = GELU(D + b1) -> bf16 tile [128 x 128] in shared memory
 //   D = H1 W2, H2, D = H2 W3, H3: 8 MMAs each (K = 128 in steps of 16)
@@ -36,14 +36,15 @@ constexpr int WB_W2 = WB_W1 + MLP_H * MLP_IN * 2;       // W2^T [128][128]
 constexpr int WB_W3 = WB_W2 + MLP_H * MLP_H * 2;        // W3^T [128][128]
 constexpr int WB_BIAS = WB_W3 + MLP_H * MLP_H * 2;      // b1, b2, b3 (128 each), b4 (32), FP32
 constexpr int WB_BYTES = WB_BIAS + (3 * MLP_H + MLP_OUT) * 4;
-constexpr int SM_X = (WB_BYTES + 127) / 128 * 128;      // two X tiles [128][16] bf16
+constexpr int NWG = 4;                                  // warpgroups per CTA
+constexpr int SM_X = (WB_BYTES + 127) / 128 * 128;      // NWG X tiles [128][16] bf16
 constexpr int X_BYTES = 128 * MLP_IN * 2;
-constexpr int SM_A = SM_X + 2 * X_BYTES;                // two H tiles [128][128] bf16
+constexpr int SM_A = SM_X + NWG * X_BYTES;              // NWG H tiles [128][128] bf16
 constexpr int A_BYTES = 128 * MLP_H * 2;
-constexpr int SM_BAR = SM_A + 2 * A_BYTES;              // two mbarriers, the TMEM address
-constexpr int SM_BYTES = SM_BAR + 32;
-constexpr int TC_THREADS = 256;
-constexpr int TMEM_COLS = 256;                          // 128 FP32 columns per warpgroup
+constexpr int SM_BAR = SM_A + NWG * A_BYTES;            // NWG mbarriers, the TMEM address
+constexpr int SM_BYTES = SM_BAR + 8 * NWG + 16;
+constexpr int TC_THREADS = 128 * NWG;
+constexpr int TMEM_COLS = 128 * NWG;                    // 128 FP32 columns per warpgroup
 constexpr long long WAIT_LIMIT = 1ll << 24;
 
 // canonical no-swizzle K-major offset of element (row, k) in a tile with K columns
@@ -116,28 +117,45 @@ __device__ __forceinline__ bool wg_all(int wg, bool v)
     return r != 0;
 }
 
-// 32 consecutive FP32 columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v)
+// N consecutive FP32 columns of this thread's TMEM lane (load and wait in one
+// statement: the destination registers are written asynchronously until the
+// wait, so no compiler-inserted copy may touch them in between)
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, uint32_t* r)
 {
-    uint32_t r[32];
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+        : "r"(taddr)
+        : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r)
+{
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
 }
 
-__device__ __forceinline__ float gelu_fast(float x)
+// GELU of two values in packed bf16x2 arithmetic (the activations are stored
+// as bf16 for the next layer anyway): 0.5 x (1 + tanh(c x (1 + a x^2)))
+__device__ __forceinline__ uint32_t gelu_bf16x2(float x0, float x1)
 {
-    float t;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(GELU_C * (x + GELU_A * x * x * x)));
-    return 0.5f * x * (1.0f + t);
+    uint32_t x, r;
+    asm("cvt.rn.bf16x2.f32 %0, %2, %1;" : "=r"(x) : "f"(x0), "f"(x1));
+    asm("{\n\t.reg .b32 x2, y, u, t, hx;\n\t"
+        "mul.rn.bf16x2 x2, %1, %1;\n\t"
+        "fma.rn.bf16x2 y, x2, %2, %3;\n\t"    // 1 + a x^2
+        "mul.rn.bf16x2 u, %1, y;\n\t"
+        "mul.rn.bf16x2 u, u, %4;\n\t"         // c x (1 + a x^2)
+        "tanh.approx.bf16x2 t, u;\n\t"
+        "mul.rn.bf16x2 hx, %1, %5;\n\t"       // x / 2
+        "fma.rn.bf16x2 %0, t, hx, hx;\n\t}\n"
+        : "=r"(r)
+        : "r"(x), "r"(0x3D373D37u), "r"(0x3F803F80u), "r"(0x3F4C3F4Cu), "r"(0x3F003F00u));
+    return r;
 }
 
 // 8 values -> 8 bf16 at a 16-byte aligned shared address
@@ -150,35 +168,35 @@ __device__ __forceinline__ void st_bf16x8(uint8_t* p, const float* v)
 }
 
 struct TcArgs {
-    // product path: features from the batch, start depths out
-    Batch b;
+    const float* feat;  // n rows of MLP_IN features
+    int64_t n;
+    // product path: start depths of intervals list[row0 + row] (list NULL: row0 + row)
     const int* list;
-    double rtol;
+    int64_t row0;
     int max_depth;
     uint32_t* starts;
-    // test path: features in, raw outputs out
-    const float* feat;
+    // test path: raw outputs
     float* out;
-    int64_t n;
     const uint8_t* w;  // weight image (WB_BYTES)
     unsigned* err;
 };
 
-template <bool FROM_BATCH>
+// STARTS: start depths out; else the raw outputs
+template <bool STARTS>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
 {
     extern __shared__ __align__(1024) uint8_t sm[];
     const int tid = threadIdx.x, wg = tid >> 7, t = tid & 127, warp = tid >> 5;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm + SM_BAR);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SM_BAR + 16);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SM_BAR + 8 * NWG);
     const float* bias = reinterpret_cast<const float*>(sm + WB_BIAS);
 
     // weights into shared memory
     for (int i = tid; i < WB_BYTES / 16; i += TC_THREADS)
         reinterpret_cast<uint4*>(sm)[i] = reinterpret_cast<const uint4*>(A.w)[i];
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[0])) : "memory");
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[1])) : "memory");
+        for (int i = 0; i < NWG; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[i])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -201,24 +219,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
     bool ok = true;
 
     const int64_t tiles = (A.n + 127) / 128;
-    for (int64_t tile = (int64_t)blockIdx.x * 2 + wg; tile < tiles && ok; tile += (int64_t)gridDim.x * 2) {
+    float4 nxt[MLP_IN / 4];
+    auto load_rows = [&](int64_t tl) {
+        const int64_t r = tl * 128 + t;
+        const float4* src = reinterpret_cast<const float4*>(A.feat + r * MLP_IN);
+#pragma unroll
+        for (int i = 0; i < MLP_IN / 4; ++i) nxt[i] = r < A.n ? src[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    };
+    load_rows((int64_t)blockIdx.x * NWG + wg);
+    for (int64_t tile = (int64_t)blockIdx.x * NWG + wg; tile < tiles && ok; tile += (int64_t)gridDim.x * NWG) {
         const int64_t row = tile * 128 + t;
         const bool live = row < A.n;
-        int64_t s = row;
-        // ---- features -> X (bf16, K-major core matrices, K = 16)
+        // ---- features -> X (bf16, K-major core matrices, K = 16); the next
+        // tile's rows are fetched now and used one iteration later
         float f[MLP_IN];
-        if constexpr (FROM_BATCH) {
-            if (live) {
-                s = A.list ? (int64_t)A.list[row] : row;
-                interval_features(A.b, s, A.rtol, f);
-            } else {
 #pragma unroll
-                for (int i = 0; i < MLP_IN; ++i) f[i] = 0.0f;
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < MLP_IN; ++i) f[i] = live ? A.feat[row * MLP_IN + i] : 0.0f;
+        for (int i = 0; i < MLP_IN / 4; ++i) {
+            f[4 * i] = nxt[i].x;
+            f[4 * i + 1] = nxt[i].y;
+            f[4 * i + 2] = nxt[i].z;
+            f[4 * i + 3] = nxt[i].w;
         }
+        load_rows(tile + (int64_t)gridDim.x * NWG);
         st_bf16x8(X + kmaj_off(t, 0, MLP_IN), f);
         st_bf16x8(X + kmaj_off(t, 8, MLP_IN), f + 8);
         fence_async_smem();
@@ -249,30 +271,40 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
             if (layer < 3) {
                 // epilogue: bias + GELU -> bf16 H (the MMAs reading H have completed)
                 const float* bl = bias + layer * MLP_H;
+                // 64 columns per TMEM load (two loads per layer)
 #pragma unroll 1
-                for (int c = 0; c < MLP_H / 32; ++c) {
-                    float v[32];
-                    tmem_ld32(tlane + 32u * c, v);
+                for (int c2 = 0; c2 < MLP_H / 64; ++c2) {
+                    uint32_t v[64];
+                    tmem_ld64(tlane + 64u * c2, v);
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) v[i] = gelu_fast(v[i] + bl[32 * c + i]);
+                    for (int half = 0; half < 2; ++half) {
+                        const int c = 2 * c2 + half;
+                        uint32_t h[16];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) st_bf16x8(H + kmaj_off(t, 32 * c + 8 * q, MLP_H), v + 8 * q);
+                        for (int i = 0; i < 16; ++i)
+                            h[i] = gelu_bf16x2(__uint_as_float(v[32 * half + 2 * i]) + bl[32 * c + 2 * i],
+                                               __uint_as_float(v[32 * half + 2 * i + 1]) + bl[32 * c + 2 * i + 1]);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            *reinterpret_cast<uint4*>(H + kmaj_off(t, 32 * c + 8 * q, MLP_H)) =
+                                make_uint4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+                    }
                 }
                 fence_async_smem();
                 fence_before();
                 wg_sync(wg);
                 fence_after();
             } else {
+                uint32_t r[32];
+                tmem_ld32(tlane, r);
                 float o[32];
-                tmem_ld32(tlane, o);
                 const float* bl = bias + 3 * MLP_H;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) o[i] += bl[i];
+                for (int i = 0; i < 32; ++i) o[i] = __uint_as_float(r[i]) + bl[i];
                 if (live) {
-                    if constexpr (FROM_BATCH) {
-                        // ellipse pieces and empty intervals keep the plain start
-                        const int64_t c = A.b.seg_curve[s];
-                        A.starts[s] = A.b.kind[c] == 0 ? 0u : quarter_depths(o, A.max_depth);
+                    if constexpr (STARTS) {
+                        const int64_t s = A.list ? (int64_t)A.list[A.row0 + row] : A.row0 + row;
+                        A.starts[s] = quarter_depths(o, A.max_depth);
                     } else {
 #pragma unroll
                         for (int i = 0; i < 32; ++i) A.out[row * MLP_OUT + i] = o[i];
@@ -305,14 +337,27 @@ int sm_count_tc()
     return n;
 }
 
-template <bool FROM_BATCH>
+// features of intervals list[row0 + r] (list NULL: row0 + r) as FP32 rows
+__global__ void k_feature_rows(Batch b, const int* list, int64_t row0, int64_t n, float rtol_feat, float* out)
+{
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = list ? (int64_t)list[row0 + r] : row0 + r;
+        float f[MLP_IN];
+        interval_features(b, s, rtol_feat, f);
+        float4* dst = reinterpret_cast<float4*>(out + r * MLP_IN);
+#pragma unroll
+        for (int i = 0; i < MLP_IN / 4; ++i) dst[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
+    }
+}
+
+template <bool STARTS>
 cudaError_t launch_tc(const TcArgs& A, cudaStream_t stream)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc<FROM_BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc<STARTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES);
     if (e != cudaSuccess) return e;
     const int64_t tiles = (A.n + 127) / 128;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tiles + 1) / 2, sm_count_tc()));
-    k_mlp_tc<FROM_BATCH><<<grid, TC_THREADS, SM_BYTES, stream>>>(A);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tiles + NWG - 1) / NWG, sm_count_tc()));
+    k_mlp_tc<STARTS><<<grid, TC_THREADS, SM_BYTES, stream>>>(A);
     return cudaGetLastError();
 }
 
@@ -354,19 +399,28 @@ cudaError_t mlp_upload_bf16(const float* host_w, void** w_dev)
 }
 
 cudaError_t mlp_starts_launch(const Batch& b, const int* list, int64_t n, const void* w_dev, double rtol, int max_depth,
-                              uint32_t* starts, cudaStream_t stream)
+                              uint32_t* starts, float* feat, int64_t feat_rows, cudaStream_t stream)
 {
-    if (n <= 0) return cudaSuccess;
-    TcArgs A{};
-    A.b = b;
-    A.list = list;
-    A.rtol = rtol;
-    A.max_depth = max_depth;
-    A.starts = starts;
-    A.n = n;
-    A.w = (const uint8_t*)w_dev;
-    A.err = (unsigned*)((uint8_t*)w_dev + WB_BYTES);
-    return launch_tc<true>(A, stream);
+    const float rf = rtol_feature(rtol);
+    for (int64_t o = 0; o < n; o += feat_rows) {
+        const int64_t m = std::min<int64_t>(feat_rows, n - o);
+        const int blocks = (int)std::min<int64_t>((m + 255) / 256, (int64_t)sm_count_tc() * 32);
+        k_feature_rows<<<blocks, 256, 0, stream>>>(b, list, o, m, rf, feat);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        TcArgs A{};
+        A.feat = feat;
+        A.n = m;
+        A.list = list;
+        A.row0 = o;
+        A.max_depth = max_depth;
+        A.starts = starts;
+        A.w = (const uint8_t*)w_dev;
+        A.err = (unsigned*)((uint8_t*)w_dev + WB_BYTES);
+        e = launch_tc<true>(A, stream);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace gcv
@@ -375,6 +429,7 @@ extern "C" gcv_status gcv_mlp_infer(const float* host_weights, const float* d_fe
 {
     using namespace gcv;
     if (!host_weights || (n > 0 && (!d_features || !d_out)) || n < 0) return GCV_ERR_INVALID;
+    if (reinterpret_cast<uintptr_t>(d_features) % 16) return GCV_ERR_INVALID;  // rows are read as float4
     if (n == 0) return GCV_OK;
     void* w = nullptr;
     cudaError_t e = mlp_upload_bf16(host_weights, &w);

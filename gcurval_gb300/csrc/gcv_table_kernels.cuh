@@ -261,11 +261,11 @@ static __global__ void k_curve_len(Batch b, Table t)
 
 // ------------------------------------------------- learned form: data
 // features of every interval (16 floats each)
-static __global__ void k_features(Batch b, double rtol, float* __restrict__ out)
+static __global__ void k_features(Batch b, float rtol_feat, float* __restrict__ out)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < b.n_seg; s += (int64_t)gridDim.x * blockDim.x) {
         float f[MLP_IN];
-        interval_features(b, s, rtol, f);
+        interval_features(b, s, rtol_feat, f);
 #pragma unroll
         for (int i = 0; i < MLP_IN; ++i) out[s * MLP_IN + i] = f[i];
     }
