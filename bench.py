@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=3,
                     help="timed steps of the plain FP64 form on the same batch, for the speed-up (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--no-graph", action="store_true",
+                    help="device-resident steps through the ordinary calls instead of the captured CUDA graph")
     ap.add_argument("--cpu-sample-curves", type=int, default=0, help="curves in the CPU-baseline sample (0: auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-curves", type=int, default=0, help="override the workload's curve count (profiling runs)")
@@ -270,8 +272,11 @@ def main():
             calc.set_learned_model(model)
 
         def step():
-            calc.createArclengthTable()
-            calc.arclengthReverseInto(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
+            if use_graph:
+                calc.stepGraph(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
+            else:
+                calc.createArclengthTable()
+                calc.arclengthReverseInto(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
 
         for _ in range(warmup):
             step()
@@ -312,6 +317,7 @@ def main():
         calc.close()
         return r
 
+    use_graph = not args.no_graph
     main_r = device_arm(precision, args.steps, max(args.warmup, 3), clocks=True, learned_on=use_learned)
     plain_r = mixed_r = None
     if precision != g.GCV_PLAIN_FP64 and args.plain_steps > 0:
@@ -444,6 +450,8 @@ def main():
                        "precision": args.precision, "rtol": batch.rtol,
                        "curves_per_gpu": n_curves, "samples_per_gpu": n_samples,
                        "l2": "flushed between timed steps (256 MB write, untimed)",
+                       "step": "one captured CUDA graph per step (gcv_step_graph)" if use_graph else
+                               "createArclengthTable + arclengthReverseInto",
                        "parallelism": f"replicas x{world} (independent curves, no collective)"},
             "samples_per_s": round(samples_per_s, 1),
             "e2e": {"value": round(world * n_curves / e2e_s, 3), "unit": "curves/s", "h2d_bytes_per_step": int(h2d),

@@ -225,8 +225,9 @@ class ArclengthCalculateGpu:
         self.close()
 
     # ------------------------------------------------------ reference API
-    def set_options(self, precision=GCV_PLAIN_FP64, rtol=None, max_depth=None, stream=None, collect_stats=False):
-        o = self._opts(precision, rtol, max_depth, stream, collect_stats)
+    def set_options(self, precision=GCV_PLAIN_FP64, rtol=None, max_depth=None, stream=None, collect_stats=False,
+                    learned=False):
+        o = self._opts(precision, rtol, max_depth, stream, collect_stats, learned)
         check(self._lib.gcv_set_options(self._h, ctypes.byref(o)))
 
     def createArclengthTable(self):
@@ -284,6 +285,25 @@ class ArclengthCalculateGpu:
         if total != n_positions:
             raise ValueError(f"sample counts add up to {total}, {n_positions} positions given")
         return total
+
+    # ------------------------------------------------------------ graph
+    def stepGraph(self, n_ptrs_for_curves, sample_position, out, is_relative=True, what=GCV_RETURN_US):
+        """createArclengthTable + arclengthReverseInto on CUDA tensors as one
+        captured CUDA graph (gcv_step_graph): captured on the first call,
+        replayed on later calls with the same tensors."""
+        for a in (n_ptrs_for_curves, sample_position, out):
+            if not _is_device(a):
+                raise ValueError("stepGraph takes CUDA tensors")
+        total = self._check_counts(n_ptrs_for_curves, int(sample_position.shape[0]))
+        width = 1 if what == GCV_RETURN_US else self.point_dim
+        if int(out.numel()) < total * width:
+            raise ValueError(f"output holds {int(out.numel())} values, {total * width} needed")
+        check(self._lib.gcv_step_graph(self._h, _ptr(n_ptrs_for_curves), _ptr(sample_position), int(bool(is_relative)),
+                                       int(what), _ptr(out)))
+        return out
+
+    def resetGraph(self):
+        check(self._lib.gcv_step_graph_reset(self._h))
 
     # ------------------------------------------------------- learned form
     def set_learned_model(self, weights):

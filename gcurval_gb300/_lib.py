@@ -56,7 +56,9 @@ class Stats(ctypes.Structure):
                 ("n_panels", ctypes.c_int64), ("n_deep_segments", ctypes.c_int64), ("n_capped", ctypes.c_int64),
                 ("n_samples", ctypes.c_int64), ("n_newton", ctypes.c_int64), ("ms_setup", ctypes.c_double),
                 ("ms_length", ctypes.c_double), ("ms_scan", ctypes.c_double), ("ms_sample", ctypes.c_double),
-                ("n_launches", ctypes.c_int64), ("ms_learned", ctypes.c_double)]
+                ("n_launches", ctypes.c_int64), ("ms_learned", ctypes.c_double),
+                ("length_blocks_per_sm", ctypes.c_int), ("sample_threads", ctypes.c_int),
+                ("sample_blocks_per_sm", ctypes.c_int), ("tuned", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -89,6 +91,8 @@ _SIGS = {
     "gcv_get_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                      ctypes.POINTER(ctypes.c_int)]),
     "gcv_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "gcv_step_graph": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, _P]),
+    "gcv_step_graph_reset": (ctypes.c_int, [_P]),
     "gcv_bspline_lengths_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
                                                    ctypes.c_double, ctypes.c_int, _P, _P]),
     # learned form (include/gcurval_gb300_learned.h)

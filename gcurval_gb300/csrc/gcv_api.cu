@@ -7,6 +7,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -113,6 +116,48 @@ int sm_count()
 
 }  // namespace
 
+// Launch shapes picked by the autotuner: persistent length workers per SM
+// (cap on the occupancy) and the sampling kernels' block size and blocks per SM.
+struct Knobs {
+    int length_cap = 32;
+    int sample_threads = 256;
+    int sample_blocks_per_sm = 64;
+    bool operator==(const Knobs& o) const
+    {
+        return length_cap == o.length_cap && sample_threads == o.sample_threads &&
+               sample_blocks_per_sm == o.sample_blocks_per_sm;
+    }
+};
+// The first TUNE_TRIALS table builds (and samplings) of a batch shape not seen
+// before in the process each run one candidate; the fastest length and
+// sampling shapes, timed by the context's events, are kept for that shape
+// (curve code, precision, learned form, log2 of the interval count).  The
+// shapes change scheduling only: every result is the same under each.
+constexpr int TUNE_TRIALS = 3;
+inline Knobs trial_knobs(int i)
+{
+    Knobs k;
+    if (i == 1) {
+        k.length_cap = 4;
+        k.sample_threads = 128;
+        k.sample_blocks_per_sm = 128;
+    } else if (i == 2) {
+        k.length_cap = 6;
+        k.sample_threads = 512;
+        k.sample_blocks_per_sm = 16;
+    }
+    return k;
+}
+struct TuneKey {
+    int code, precision, learned, log_seg;
+    bool operator<(const TuneKey& o) const
+    {
+        return std::tie(code, precision, learned, log_seg) < std::tie(o.code, o.precision, o.learned, o.log_seg);
+    }
+};
+static std::mutex g_tune_m;
+static std::map<TuneKey, Knobs> g_tuned;
+
 constexpr int64_t LEARNED_CHUNK = 1 << 24;  // intervals per feature chunk of the learned form (1 GiB)
 constexpr int STREAM_EVENTS = 4;  // host-buffer sampling: events per stage, used round robin
 
@@ -172,6 +217,24 @@ struct gcv_ctx {
     std::vector<double> h_len;
     bool h_len_valid = false;
     unsigned long long* h_ctr = nullptr;  // pinned
+    // one-call steps captured as a CUDA graph (gcv_step_graph)
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    cudaStream_t gstream = nullptr;  // capture stream when the context uses the legacy stream
+    struct {
+        const int* counts;
+        const double* pos;
+        double* out;
+        int is_relative, what, learned;
+        gcv_options opt;
+    } gargs{};
+    DBuf<int64_t> scan_blk;
+    int64_t graph_kernels = 0;
+    Knobs knobs, gknobs;  // launch shapes in use / in the captured step
+    // autotuner progress of this context (-1: tuned, shapes from the table)
+    int len_trial = 0, smp_trial = 0;
+    double len_ms[TUNE_TRIALS] = {}, smp_ms[TUNE_TRIALS] = {};
+    TuneKey tune_key{-9, -9, -9, -9};
     // chunked host <-> device streaming of samples
     cudaStream_t s_in = nullptr, s_out = nullptr;
     cudaEvent_t ev_in[STREAM_EVENTS] = {}, ev_done[STREAM_EVENTS] = {}, ev_out[STREAM_EVENTS] = {};
@@ -291,6 +354,10 @@ void destroy_ctx(gcv_ctx* c)
         if (c->ev_done[k]) cudaEventDestroy(c->ev_done[k]);
         if (c->ev_out[k]) cudaEventDestroy(c->ev_out[k]);
     }
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    if (c->gstream) cudaStreamDestroy(c->gstream);
+    c->scan_blk.release();
     if (c->s_in) cudaStreamDestroy(c->s_in);
     if (c->s_out) cudaStreamDestroy(c->s_out);
     for (auto& e : c->ev)
@@ -556,17 +623,17 @@ gcv_status launch_length_code(gcv_ctx* c, int code, const LengthParams& P)
     if constexpr (MODE == 0) {
         switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: e = length_launch<0, C, PREC>(P, c->stream, sms); break;
+    case C: e = length_launch<0, C, PREC>(P, c->stream, sms, c->knobs.length_cap); break;
             GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
         default: return fail(GCV_ERR_INVALID, "no length kernel for curve code " + std::to_string(code));
         }
     } else {
         switch (code) {
-        case CODE_ELLIPSE: e = length_launch<MODE, CODE_ELLIPSE, PREC>(P, c->stream, sms); break;
-        case bs_code(3, 2): e = length_launch<MODE, bs_code(3, 2), PREC>(P, c->stream, sms); break;
-        case bs_code(3, 3): e = length_launch<MODE, bs_code(3, 3), PREC>(P, c->stream, sms); break;
-        default: e = length_launch<MODE, -1, PREC>(P, c->stream, sms); break;
+        case CODE_ELLIPSE: e = length_launch<MODE, CODE_ELLIPSE, PREC>(P, c->stream, sms, c->knobs.length_cap); break;
+        case bs_code(3, 2): e = length_launch<MODE, bs_code(3, 2), PREC>(P, c->stream, sms, c->knobs.length_cap); break;
+        case bs_code(3, 3): e = length_launch<MODE, bs_code(3, 3), PREC>(P, c->stream, sms, c->knobs.length_cap); break;
+        default: e = length_launch<MODE, -1, PREC>(P, c->stream, sms, c->knobs.length_cap); break;
         }
     }
     if (e != cudaSuccess) return cuda_fail(e, "length kernel launch");
@@ -602,6 +669,88 @@ gcv_status launch_main_pass(gcv_ctx* c, LengthParams P)
     return GCV_OK;
 }
 
+// ---------------------------------------------------------- autotuner
+TuneKey tune_key_of(gcv_ctx* c)
+{
+    int lg = 0;
+    for (int64_t n = c->n_seg; n > 1; n >>= 1) ++lg;
+    return TuneKey{c->code, c->opt.precision, c->opt.learned && c->mlp_w ? 1 : 0, lg};
+}
+
+// launch shapes for the next table build / sampling of this context
+void select_knobs(gcv_ctx* c)
+{
+    const TuneKey key = tune_key_of(c);
+    if (c->tune_key < key || key < c->tune_key) {  // a new shape: start over
+        c->tune_key = key;
+        c->len_trial = c->smp_trial = 0;
+    }
+    {
+        std::lock_guard<std::mutex> g(g_tune_m);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) {
+            c->knobs = it->second;
+            c->len_trial = c->smp_trial = -1;
+            return;
+        }
+    }
+    if (c->len_trial >= 0 && c->len_trial < TUNE_TRIALS) c->knobs.length_cap = trial_knobs(c->len_trial).length_cap;
+    if (c->smp_trial >= 0 && c->smp_trial < TUNE_TRIALS) {
+        const Knobs k = trial_knobs(c->smp_trial);
+        c->knobs.sample_threads = k.sample_threads;
+        c->knobs.sample_blocks_per_sm = k.sample_blocks_per_sm;
+    }
+}
+
+int argmin3(const double* v)
+{
+    int b = 0;
+    for (int i = 1; i < TUNE_TRIALS; ++i)
+        if (v[i] < v[b]) b = i;
+    return b;
+}
+
+void tune_finish_if_done(gcv_ctx* c)
+{
+    if (c->len_trial == TUNE_TRIALS && c->smp_trial == TUNE_TRIALS) {
+        Knobs k;
+        k.length_cap = trial_knobs(argmin3(c->len_ms)).length_cap;
+        const Knobs ks = trial_knobs(argmin3(c->smp_ms));
+        k.sample_threads = ks.sample_threads;
+        k.sample_blocks_per_sm = ks.sample_blocks_per_sm;
+        std::lock_guard<std::mutex> g(g_tune_m);
+        g_tuned[c->tune_key] = k;
+        c->knobs = k;
+        c->len_trial = c->smp_trial = -1;
+    }
+}
+
+// record the length passes' time (events ev[6] -> ev[2]) of a tuning build
+gcv_status tune_after_table(gcv_ctx* c)
+{
+    if (c->len_trial < 0 || c->len_trial >= TUNE_TRIALS) return GCV_OK;
+    CU(cudaEventSynchronize(c->ev[2]));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, c->ev[6], c->ev[2]));
+    c->len_ms[c->len_trial++] = ms;
+    if (c->len_trial == TUNE_TRIALS && c->smp_trial >= 0 && c->smp_trial < TUNE_TRIALS)
+        c->knobs.length_cap = trial_knobs(argmin3(c->len_ms)).length_cap;
+    tune_finish_if_done(c);
+    return GCV_OK;
+}
+
+// record the sampling time (ev[4] -> ev[5]) of a tuning sampling call
+gcv_status tune_after_sampling(gcv_ctx* c)
+{
+    if (c->smp_trial < 0 || c->smp_trial >= TUNE_TRIALS) return GCV_OK;
+    CU(cudaEventSynchronize(c->ev[5]));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, c->ev[4], c->ev[5]));
+    c->smp_ms[c->smp_trial++] = ms;
+    tune_finish_if_done(c);
+    return GCV_OK;
+}
+
 gcv_status launch_setup_list(gcv_ctx* c, const CodeRange& r)
 {
     const int64_t n = r.end - r.begin;
@@ -624,6 +773,7 @@ gcv_status launch_setup_list(gcv_ctx* c, const CodeRange& r)
 
 gcv_status build_table(gcv_ctx* c)
 {
+    select_knobs(c);
     CHECK(ensure_table_buffers(c));
     const bool mixed = c->opt.precision == GCV_MIXED;
     const Batch b = batch_view(c);
@@ -666,7 +816,7 @@ gcv_status build_table(gcv_ctx* c)
         // keep the set-up's error bits, clear the rest
         CU(cudaMemsetAsync(c->ctr.p, 0, C_ERR * sizeof(unsigned long long), c->stream));
         CU(cudaMemsetAsync(c->ctr.p + C_WORK_CODE, 0, (C_COUNT - C_WORK_CODE) * sizeof(unsigned long long), c->stream));
-        LengthParams P;
+        LengthParams P{};
         P.b = b;
         P.t = table_view(c);
         P.rtol = c->opt.rtol;
@@ -752,6 +902,7 @@ gcv_status build_table(gcv_ctx* c)
         if (err) return fail(GCV_ERR_TIMEOUT, "network inference: a tensor-core wait gave up");
     }
     c->learned_ran = learned;
+    CHECK(tune_after_table(c));
     return GCV_OK;
 }
 
@@ -759,14 +910,15 @@ gcv_status build_table(gcv_ctx* c)
 
 gcv_status launch_sampler(gcv_ctx* c, int code, const SampleParams& P, int64_t n)
 {
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + SAMPLE_THREADS - 1) / SAMPLE_THREADS,
-                                                               (int64_t)sm_count() * 64));
+    const int th = c->knobs.sample_threads;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((n + th - 1) / th,
+                                                               (int64_t)sm_count() * c->knobs.sample_blocks_per_sm));
     const bool mixed = c->opt.precision == GCV_MIXED;
     const float2* cf = c->coef_ff.p;
     cudaError_t e = cudaErrorInvalidValue;
     switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: e = mixed ? sample_launch<C, 1>(P, cf, c->stream, grid) : sample_launch<C, 0>(P, cf, c->stream, grid); break;
+    case C: e = mixed ? sample_launch<C, 1>(P, cf, c->stream, grid, th) : sample_launch<C, 0>(P, cf, c->stream, grid, th); break;
         GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
     default: return fail(GCV_ERR_INVALID, "no sampling kernel for curve code " + std::to_string(code));
@@ -827,7 +979,7 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, 
     const int width = what == GCV_RETURN_US ? 1 : c->point_dim;
     CU(cudaEventRecord(c->ev[4], c->stream));
     if (c->opt.collect_stats) CU(cudaMemsetAsync(c->ctr.p + C_NEWTON, 0, sizeof(unsigned long long), c->stream));
-    SampleParams P;
+    SampleParams P{};
     P.b = batch_view(c);
     P.t = table_view(c);
     P.sample_off = d_sample_off;
@@ -916,7 +1068,147 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, 
     CU(cudaEventRecord(c->ev[5], c->stream));
     c->ev_sample = true;
     c->stats.n_samples = total;
+    CHECK(tune_after_sampling(c));
     return GCV_OK;
+}
+
+// ---------------------------------------------------------- graph step
+// The table build and the sampling without host synchronisation, for stream
+// capture: the deep passes read their item count on the device, the sample
+// offsets are scanned on the device, the sampling launches read their ranges
+// on the device.  Pools keep the sizes an ordinary build gave them; an
+// overflow is reported through the error word after the replay.
+gcv_status enqueue_table_graph(gcv_ctx* c)
+{
+    const bool mixed = c->opt.precision == GCV_MIXED;
+    const Batch b = batch_view(c);
+    CU(cudaEventRecord(c->ev[0], c->stream));
+    CU(cudaMemsetAsync(c->ctr.p, 0, C_COUNT * sizeof(unsigned long long), c->stream));
+    if (c->n_seg > 0 && c->code >= 0) {
+        const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 64));
+        k_setup<<<blocks, 256, 0, c->stream>>>(b, table_view(c));
+        CU(cudaGetLastError());
+    } else if (c->n_seg > 0) {
+        for (const CodeRange& r : c->code_ranges) CHECK(launch_setup_list(c, r));
+    }
+    CU(cudaEventRecord(c->ev[1], c->stream));
+    const bool learned = c->opt.learned && c->mlp_w && c->n_seg > 0;
+    if (learned) {
+        CU(cudaMemsetAsync(c->starts.p, 0, (size_t)c->n_seg * sizeof(uint32_t), c->stream));
+        const int md = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
+        const int64_t rows = std::min<int64_t>(c->n_seg, LEARNED_CHUNK);
+        auto run = [&](const int* list, int64_t n) -> gcv_status {
+            cudaError_t e = mlp_starts_launch(b, list, n, c->mlp_w, c->opt.rtol, md, c->starts.p, c->feat.p, rows,
+                                              c->stream);
+            if (e != cudaSuccess) return cuda_fail(e, "network inference");
+            return GCV_OK;
+        };
+        if (c->code > 0) {
+            CHECK(run(nullptr, c->n_seg));
+        } else if (c->code < 0) {
+            for (const CodeRange& r : c->code_ranges)
+                if (r.code != CODE_ELLIPSE) CHECK(run(c->seg_list.p + r.begin, r.end - r.begin));
+        }
+    }
+    CU(cudaEventRecord(c->ev[6], c->stream));
+    if (c->n_seg > 0) {
+        LengthParams P{};
+        P.b = b;
+        P.t = table_view(c);
+        P.rtol = c->opt.rtol;
+        P.max_depth = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
+        P.collect = c->opt.collect_stats;
+        P.coef_ff = c->coef_ff.p;
+        P.starts = learned ? c->starts.p : nullptr;
+        CHECK(launch_main_pass(c, P));
+        // deep passes over the deep list, its length read on the device
+        LengthParams Q = P;
+        Q.list = c->deep_list.p;
+        Q.n_items = (int64_t)c->deep_list.n;
+        Q.n_items_dev = c->ctr.p + C_DEEP;
+        Q.work = c->ctr.p + C_WORK;
+        Q.starts = nullptr;
+        Q.collect = 0;
+        CU(cudaMemsetAsync(c->ctr.p + C_WORK, 0, sizeof(unsigned long long), c->stream));
+        CHECK(launch_length<1>(c, c->code, Q));
+        Q.collect = P.collect;
+        CU(cudaMemsetAsync(c->ctr.p + C_WORK, 0, sizeof(unsigned long long), c->stream));
+        CHECK(launch_length<2>(c, c->code, Q));
+    }
+    CU(cudaEventRecord(c->ev[2], c->stream));
+    const int64_t tiles = (c->n_seg + SCAN_TILE - 1) / SCAN_TILE;
+    if (tiles > 0) {
+        CU(cudaMemsetAsync(c->scan_status.p, 0, (size_t)tiles * sizeof(int), c->stream));
+        k_scan<<<(unsigned)tiles, SCAN_THREADS, 0, c->stream>>>(b, table_view(c), tiles);
+        CU(cudaGetLastError());
+    }
+    if (c->n_curve > 0) {
+        k_curve_len<<<(unsigned)std::min<int64_t>((c->n_curve + 255) / 256, 65535), 256, 0, c->stream>>>(b, table_view(c));
+        CU(cudaGetLastError());
+    }
+    CU(cudaEventRecord(c->ev[3], c->stream));
+    return GCV_OK;
+}
+
+// exclusive prefix of the counts (gathered through idx when set) into out[0..n]
+gcv_status enqueue_count_scan(gcv_ctx* c, const int* counts, const int* idx, int64_t* out)
+{
+    const int64_t n = c->n_curve;
+    if (n == 0) return GCV_OK;
+    const int64_t nb = (n + 1023) / 1024;
+    k_count_block_sums<<<(unsigned)nb, 1024, 0, c->stream>>>(counts, idx, n, c->scan_blk.p, c->ctr.p + C_ERR);
+    k_count_scan_blocks<<<1, 32, 0, c->stream>>>(c->scan_blk.p, nb);
+    k_count_scan<<<(unsigned)nb, 1024, 0, c->stream>>>(counts, idx, n, c->scan_blk.p, out);
+    CU(cudaGetLastError());
+    return GCV_OK;
+}
+
+gcv_status enqueue_sampling_graph(gcv_ctx* c, const int* d_counts, const double* d_pos, int is_relative, int what,
+                                  double* d_out)
+{
+    CU(cudaEventRecord(c->ev[4], c->stream));
+    if (c->n_curve == 0) {
+        CU(cudaEventRecord(c->ev[5], c->stream));
+        return GCV_OK;
+    }
+    CHECK(enqueue_count_scan(c, d_counts, nullptr, c->sample_off.p));
+    SampleParams P{};
+    P.b = batch_view(c);
+    P.t = table_view(c);
+    P.sample_off = c->sample_off.p;
+    P.pos = d_pos;
+    P.is_relative = is_relative;
+    P.what = what;
+    P.pdim = c->point_dim;
+    P.out = d_out;
+    P.collect = c->opt.collect_stats;
+    P.rtol = c->opt.rtol;
+    // grids for any sample count: the kernels loop over their ranges
+    const int64_t nominal = (int64_t)sm_count() * c->knobs.sample_blocks_per_sm * c->knobs.sample_threads;
+    if (c->code >= 0) {
+        P.s_begin = 0;
+        P.s_end_dev = c->sample_off.p + c->n_curve;
+        CHECK(launch_sampler(c, c->code, P, nominal));
+    } else {
+        CHECK(enqueue_count_scan(c, d_counts, c->curve_list.p, c->list_sample_off.p));
+        P.curve_list = c->curve_list.p;
+        P.list_off = c->list_sample_off.p;
+        for (const CodeRange& r : c->curve_ranges) {
+            P.cb = r.begin;
+            P.ce = r.end;
+            CHECK(launch_sampler(c, r.code, P, nominal));
+        }
+    }
+    CU(cudaEventRecord(c->ev[5], c->stream));
+    return GCV_OK;
+}
+
+void drop_graph(gcv_ctx* c)
+{
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->gexec = nullptr;
+    c->graph = nullptr;
 }
 
 gcv_status stage_counts(gcv_ctx* c, const int* n_ptrs, int in_where, int64_t* total)
@@ -1302,6 +1594,10 @@ gcv_status gcv_get_stats(gcv_ctx* ctx, gcv_stats* out)
         }
     }
     cudaGetLastError();
+    ctx->stats.length_blocks_per_sm = ctx->knobs.length_cap;
+    ctx->stats.sample_threads = ctx->knobs.sample_threads;
+    ctx->stats.sample_blocks_per_sm = ctx->knobs.sample_blocks_per_sm;
+    ctx->stats.tuned = ctx->len_trial < 0 ? 1 : 0;
     *out = ctx->stats;
     return GCV_OK;
 }
@@ -1352,6 +1648,120 @@ gcv_status gcv_get_shape(gcv_ctx* ctx, int64_t* n_curve, int64_t* n_segments, in
     return GCV_OK;
 }
 
+gcv_status gcv_step_graph(gcv_ctx* ctx, const int* d_counts, const double* d_pos, int is_relative, int what,
+                          double* d_out)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    if (what != GCV_RETURN_US && what != GCV_RETURN_POINTS) return fail(GCV_ERR_INVALID, "what must be RETURN_US or RETURN_POINTS");
+    if (ctx->n_curve > 0 && (!d_counts || !d_pos || !d_out)) return fail(GCV_ERR_INVALID, "NULL device buffer");
+    gcv_ctx* c = ctx;
+    // an ordinary build first: it sizes the leaf pool and the deep list
+    if (!c->table_ready) {
+        CHECK(build_table(c));
+        c->table_ready = true;
+        c->h_len_valid = false;
+    }
+    select_knobs(c);
+    const bool same = c->gexec && c->gknobs == c->knobs && c->gargs.counts == d_counts && c->gargs.pos == d_pos && c->gargs.out == d_out &&
+                      c->gargs.is_relative == is_relative && c->gargs.what == what &&
+                      c->gargs.learned == (c->opt.learned && c->mlp_w ? 1 : 0) &&
+                      std::memcmp(&c->gargs.opt, &c->opt, sizeof(gcv_options)) == 0;
+    if (!same) {
+        drop_graph(c);
+        CHECK(c->sample_off.reserve((size_t)c->n_curve + 1));
+        CHECK(c->list_sample_off.reserve((size_t)c->n_curve + 1));
+        CHECK(c->scan_blk.reserve((size_t)(c->n_curve + 1023) / 1024 + 1));
+        if (c->opt.learned && c->mlp_w) {
+            CHECK(c->starts.reserve((size_t)std::max<int64_t>(c->n_seg, 1)));
+            CHECK(c->feat.reserve((size_t)std::min<int64_t>(std::max<int64_t>(c->n_seg, 1), LEARNED_CHUNK) * MLP_IN));
+        }
+        if (!c->stream && !c->gstream) CU(cudaStreamCreateWithFlags(&c->gstream, cudaStreamNonBlocking));
+        cudaStream_t user = c->stream;
+        cudaStream_t cap = c->stream ? c->stream : c->gstream;
+        CU(cudaStreamSynchronize(user));
+        c->stream = cap;
+        cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+        gcv_status st = e == cudaSuccess ? GCV_OK : cuda_fail(e, "cudaStreamBeginCapture");
+        if (st == GCV_OK) st = enqueue_table_graph(c);
+        if (st == GCV_OK) st = enqueue_sampling_graph(c, d_counts, d_pos, is_relative, what, d_out);
+        cudaGraph_t g = nullptr;
+        e = cudaStreamEndCapture(cap, &g);
+        c->stream = user;
+        if (st != GCV_OK) {
+            if (g) cudaGraphDestroy(g);
+            return st;
+        }
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        c->graph = g;
+        e = cudaGraphInstantiate(&c->gexec, g, 0);
+        if (e != cudaSuccess) {
+            drop_graph(c);
+            return cuda_fail(e, "cudaGraphInstantiate");
+        }
+        c->gargs.counts = d_counts;
+        c->gargs.pos = d_pos;
+        c->gargs.out = d_out;
+        c->gargs.is_relative = is_relative;
+        c->gargs.what = what;
+        c->gargs.learned = c->opt.learned && c->mlp_w ? 1 : 0;
+        std::memcpy(&c->gargs.opt, &c->opt, sizeof(gcv_options));
+        c->gknobs = c->knobs;
+        // kernels per replay, for the launch count
+        size_t nn = 0;
+        c->graph_kernels = 0;
+        if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
+            std::vector<cudaGraphNode_t> nodes(nn);
+            if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+                for (cudaGraphNode_t nd : nodes) {
+                    cudaGraphNodeType ty;
+                    if (cudaGraphNodeGetType(nd, &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel) c->graph_kernels++;
+                }
+        }
+    }
+    CU(cudaGraphLaunch(c->gexec, c->stream));
+    c->stats.n_launches += c->graph_kernels;
+    CHECK(read_counters(c));
+    unsigned long long err = c->h_ctr[C_ERR];
+    if (c->gargs.learned) {
+        unsigned werr = 0;
+        CU(cudaMemcpy(&werr, (uint8_t*)c->mlp_w + mlp_dev_bytes(), sizeof(werr), cudaMemcpyDeviceToHost));
+        if (werr) return fail(GCV_ERR_TIMEOUT, "network inference: a tensor-core wait gave up");
+    }
+    if (err & ERR_BAD_KNOTS) return fail(GCV_ERR_INVALID, "knot vector decreases or holds NaN");
+    if (err & ERR_BAD_COUNT) return fail(GCV_ERR_INVALID, "negative sample count");
+    if (err & ERR_SCAN_TIMEOUT) return fail(GCV_ERR_TIMEOUT, "scan look-back gave up");
+    if (err & (ERR_POOL | ERR_DEEP_LIST)) {
+        // the pools were too small for this data: the ordinary path grows them,
+        // and the next call captures again
+        drop_graph(c);
+        CHECK(build_table(c));
+        int64_t total = 0;
+        CHECK(stage_counts(c, d_counts, GCV_DEVICE, &total));
+        CHECK(run_sampling(c, c->sample_off.p, const_cast<double*>(d_pos), total, is_relative, what, d_out));
+        CU(cudaStreamSynchronize(c->stream));
+        c->h_len_valid = false;
+        return GCV_OK;
+    }
+    c->ev_table = c->ev_sample = true;
+    c->learned_ran = c->gargs.learned != 0;
+    c->stats.n_leaves = (int64_t)c->h_ctr[C_LEAF_TOP];
+    c->stats.n_deep_segments = (int64_t)c->h_ctr[C_DEEP];
+    c->stats.n_panels = (int64_t)c->h_ctr[C_PANELS];
+    c->stats.n_capped = (int64_t)c->h_ctr[C_CAPPED];
+    c->stats.n_newton = (int64_t)c->h_ctr[C_NEWTON];
+    c->h_len_valid = false;
+    CHECK(tune_after_table(c));
+    CHECK(tune_after_sampling(c));
+    return GCV_OK;
+}
+
+gcv_status gcv_step_graph_reset(gcv_ctx* ctx)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    drop_graph(ctx);
+    return GCV_OK;
+}
+
 gcv_status gcv_learned_features(gcv_ctx* ctx, float* d_features)
 {
     if (!ctx || (!d_features && ctx->n_seg > 0)) return fail(GCV_ERR_INVALID, "NULL argument");
@@ -1383,6 +1793,7 @@ gcv_status gcv_set_learned_model(gcv_ctx* ctx, const float* host_weights)
 {
     if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
     CU(cudaStreamSynchronize(ctx->stream));
+    drop_graph(ctx);  // a captured step holds the old weights
     if (ctx->mlp_w) {
         cudaFree(ctx->mlp_w);
         ctx->mlp_w = nullptr;

@@ -101,6 +101,7 @@ struct SampleParams {
     const int64_t* list_off;
     int64_t cb, ce;
     int64_t s_begin, s_end;  // sample range of the launch when curve_list is NULL
+    const int64_t* s_end_dev;  // when set: the end of that range, read on the device
 };
 
 // Sample range of a launch and, for launch-local sample i, its curve and its
@@ -108,7 +109,7 @@ struct SampleParams {
 __device__ __forceinline__ void sample_range(const SampleParams& P, int64_t& i0, int64_t& i1)
 {
     i0 = P.curve_list ? P.list_off[P.cb] : P.s_begin;
-    i1 = P.curve_list ? P.list_off[P.ce] : P.s_end;
+    i1 = P.curve_list ? P.list_off[P.ce] : (P.s_end_dev ? *P.s_end_dev : P.s_end);
 }
 __device__ __forceinline__ int sample_curve(const SampleParams& P, int64_t i, int64_t& gi)
 {
@@ -122,7 +123,8 @@ __device__ __forceinline__ int sample_curve(const SampleParams& P, int64_t i, in
     return upper_bound_i64(P.sample_off, int(P.b.n_curve) + 1, i);
 }
 
-constexpr int SAMPLE_THREADS = 256;
+constexpr int SAMPLE_THREADS = 256;      // default block size
+constexpr int SAMPLE_THREADS_MAX = 512;  // largest block size the autotuner tries
 constexpr int NEWTON_MAXIT = 16;
 
 template <int CODE>
@@ -202,7 +204,7 @@ __device__ __forceinline__ double leaf_newton(const double* __restrict__ seg, do
 }
 
 template <int CODE>
-__global__ void __launch_bounds__(SAMPLE_THREADS) k_sample(SampleParams P)
+__global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample(SampleParams P)
 {
     const Batch& b = P.b;
     const Table& t = P.t;

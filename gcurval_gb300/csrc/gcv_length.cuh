@@ -41,18 +41,20 @@ struct LengthParams {
     int collect;
     const int* list;  // segments to process; NULL: segments 0 .. n_items - 1
     int64_t n_items;
+    const unsigned long long* n_items_dev;  // when set: the item count, read on the device
+                                            // (graph launches; n_items then sizes the grid)
     const float2* coef_ff;  // float-float copy of the coefficients (PREC 1)
     unsigned long long* work;  // work-queue head of this launch (starts at 0)
     const uint32_t* starts;    // learned quarter start depths per segment (NULL: plain walk)
 };
 
 // Launches k_length<MODE, CODE, PREC> over P (persistent grid sized from the
-// occupancy and sm_count); defined with the kernel in gcv_length_impl.cuh and
+// occupancy, capped at blocks_per_sm_cap per SM, and sm_count); defined with the kernel in gcv_length_impl.cuh and
 // instantiated per curve code in the gcv_len_*.cu units.
 //   MODE 0: main pass; MODE 1: count pass of the deep list; MODE 2: write pass.
 //   CODE: curve code, or -1 for runtime dispatch per segment.
 //   PREC 0: FP64 panels; 1: float-float panels.
 template <int MODE, int CODE, int PREC>
-cudaError_t length_launch(const LengthParams& P, cudaStream_t stream, int sm_count);
+cudaError_t length_launch(const LengthParams& P, cudaStream_t stream, int sm_count, int blocks_per_sm_cap);
 
 }  // namespace gcv

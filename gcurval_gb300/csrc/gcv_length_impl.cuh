@@ -97,6 +97,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
     // (FP64: 2^-52; float-float: ~2^-46)
     const double eps50 = PREC == 1 ? 50.0 * 1.4210854715202004e-14 : 50.0 * 2.220446049250313e-16;
 
+    const int64_t n_items = P.n_items_dev ? (int64_t)*P.n_items_dev : P.n_items;
     bool active = false, exhausted = false;
     int64_t s = 0, pool = 0;
     int code = CODE >= 0 ? CODE : 0;
@@ -123,7 +124,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
             base = __shfl_sync(FULL, base, leader);
             if (need) {
                 const int64_t item = (int64_t)base + __popc(m & lt_mask);
-                if (item >= P.n_items) {
+                if (item >= n_items) {
                     exhausted = true;
                 } else {
                     s = P.list ? (int64_t)P.list[item] : item;
@@ -347,12 +348,13 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
 }
 
 template <int MODE, int CODE, int PREC>
-cudaError_t length_launch(const LengthParams& P, cudaStream_t stream, int sm_count)
+cudaError_t length_launch(const LengthParams& P, cudaStream_t stream, int sm_count, int blocks_per_sm_cap)
 {
     int occ = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_length<MODE, CODE, PREC>, LK_THREADS, 0);
     if (e != cudaSuccess) return e;
-    occ = occ < 1 ? 1 : (occ > 32 ? 32 : occ);
+    const int cap = blocks_per_sm_cap < 1 ? 1 : blocks_per_sm_cap;
+    occ = occ < 1 ? 1 : (occ > cap ? cap : occ);
     // persistent: fill the GPU, but no more lanes than there are intervals
     const int64_t want = (P.n_items + LK_THREADS - 1) / LK_THREADS;
     int64_t grid = (int64_t)sm_count * occ;
@@ -363,7 +365,7 @@ cudaError_t length_launch(const LengthParams& P, cudaStream_t stream, int sm_cou
 }
 
 #define GCV_LENGTH_INST(MODE, CODE, PREC)                                                          \
-    template cudaError_t length_launch<MODE, CODE, PREC>(const LengthParams&, cudaStream_t, int);
+    template cudaError_t length_launch<MODE, CODE, PREC>(const LengthParams&, cudaStream_t, int, int);
 // both precisions of one (MODE, CODE)
 #define GCV_LENGTH_INST2(MODE, CODE) GCV_LENGTH_INST(MODE, CODE, 0) GCV_LENGTH_INST(MODE, CODE, 1)
 

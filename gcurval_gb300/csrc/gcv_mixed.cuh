@@ -101,7 +101,7 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
 // (G8 partial integral on the shorter side, local to the leaf), and the
 // final update of v in FP64.
 template <int CODE>
-__global__ void __launch_bounds__(SAMPLE_THREADS) k_sample_ff(SampleParams P, const float2* __restrict__ coef_ff)
+__global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample_ff(SampleParams P, const float2* __restrict__ coef_ff)
 {
     const Batch& b = P.b;
     const Table& t = P.t;

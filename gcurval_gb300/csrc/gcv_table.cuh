@@ -37,7 +37,7 @@ enum Counter {
     C_WORK_CODE = 16,   // work-queue heads of the per-code main-pass launches
     C_COUNT = 32
 };
-enum ErrBits { ERR_POOL = 1, ERR_SCAN_TIMEOUT = 2, ERR_BAD_KNOTS = 4, ERR_DEEP_LIST = 8 };
+enum ErrBits { ERR_POOL = 1, ERR_SCAN_TIMEOUT = 2, ERR_BAD_KNOTS = 4, ERR_DEEP_LIST = 8, ERR_BAD_COUNT = 16 };
 
 struct Table {
     double* coef;      // per-segment evaluation data (code_stride doubles), FP64 path

@@ -259,6 +259,75 @@ static __global__ void k_curve_len(Batch b, Table t)
     }
 }
 
+// ------------------------------------------- sample offsets on the device
+// Exclusive prefix sums of n int32 sample counts, read through idx when set
+// (counts of the curves idx[0..n) in that order), into out[0..n]; out[n] is
+// the total.  Three launches: block totals (1024 counts per block), a serial
+// scan of the block totals, block-local scans.  Negative counts count as 0
+// and raise ERR_BAD_COUNT.
+static __global__ void k_count_block_sums(const int* cnt, const int* idx, int64_t n, int64_t* blk, unsigned long long* err)
+{
+    __shared__ int64_t w[32];
+    const int64_t base = (int64_t)blockIdx.x * 1024;
+    int64_t x = 0;
+    for (int i = threadIdx.x; i < 1024; i += blockDim.x)
+        if (base + i < n) {
+            const int v = cnt[idx ? idx[base + i] : base + i];
+            if (v < 0) atomicOr(err, (unsigned long long)ERR_BAD_COUNT);
+            x += v > 0 ? v : 0;
+        }
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t t = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += w[i];
+        blk[blockIdx.x] = t;
+    }
+}
+static __global__ void k_count_scan_blocks(int64_t* blk, int64_t nb)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int64_t run = 0;
+        for (int64_t i = 0; i < nb; ++i) {
+            const int64_t v = blk[i];
+            blk[i] = run;
+            run += v;
+        }
+        blk[nb] = run;
+    }
+}
+static __global__ void __launch_bounds__(1024) k_count_scan(const int* cnt, const int* idx, int64_t n, const int64_t* blk,
+                                                            int64_t* out)
+{
+    __shared__ int64_t w[32];
+    const int64_t i = (int64_t)blockIdx.x * 1024 + threadIdx.x;
+    int64_t x = 0;
+    if (i < n) {
+        const int v = cnt[idx ? idx[i] : i];
+        x = v > 0 ? v : 0;
+    }
+    int64_t v = x;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int d = 1; d < 32; d <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += y;
+    }
+    if (lane == 31) w[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        int64_t t = w[lane];
+        for (int d = 1; d < 32; d <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, t, d);
+            if (lane >= d) t += y;
+        }
+        w[lane] = t;
+    }
+    __syncthreads();
+    if (i < n) out[i] = blk[blockIdx.x] + (wid ? w[wid - 1] : 0) + v - x;
+    if (i == n - 1) out[n] = blk[gridDim.x];
+}
+
 // ------------------------------------------------- learned form: data
 // features of every interval (16 floats each)
 static __global__ void k_features(Batch b, float rtol_feat, float* __restrict__ out)

@@ -110,6 +110,10 @@ typedef struct gcv_stats {
     double ms_setup, ms_length, ms_scan, ms_sample;  /* device time per phase */
     int64_t n_launches;       /* kernels launched by the context so far */
     double ms_learned;        /* network inference inside ms_length (learned form) */
+    /* launch shapes in use, picked by the autotuner: the first three table
+       builds and samplings of a batch shape new to the process each try one
+       candidate, later ones use the fastest (tuned = 1) */
+    int length_blocks_per_sm, sample_threads, sample_blocks_per_sm, tuned;
 } gcv_stats;
 
 const char* gcv_status_string(gcv_status s);
@@ -198,6 +202,24 @@ gcv_status gcv_arclength_reverse_into(gcv_ctx* ctx, const int* n_ptrs_for_curves
                                       int in_where, int what, double* out, int out_where);
 
 gcv_status gcv_free_result(gcv_result* result);
+
+/* createArclengthTable followed by arclengthReverse of device-resident
+ * counts / positions into device memory, as one CUDA graph on the context's
+ * stream.  The first call builds the table the ordinary way (which sizes the
+ * leaf pool and the deep list), captures the whole step - set-up, network
+ * inference when the learned form is on, the length passes with their item
+ * counts read on the device, the scan, a device scan of the sample counts
+ * and the sampling launches - and replays it; later calls with the same
+ * buffers, flags and options only replay it (a change captures again).
+ * The counts' and positions' contents may change between calls.  A replay
+ * whose data outgrew the pools is redone the ordinary way, which grows them,
+ * and the next call captures again.  No reference counterpart: the reference
+ * synchronises with the host after every kernel
+ * (gcurval/detail/cuda/arclength_calculate.h:259-323). */
+gcv_status gcv_step_graph(gcv_ctx* ctx, const int* d_counts, const double* d_pos, int is_relative,
+                          int what, double* d_out);
+/* Drops the captured step (the next gcv_step_graph captures again). */
+gcv_status gcv_step_graph_reset(gcv_ctx* ctx);
 
 /* clearArclength (arclength_calculate.h:233-237): drops the cached lengths. */
 gcv_status gcv_clear_arclength(gcv_ctx* ctx);
