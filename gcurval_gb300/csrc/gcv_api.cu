@@ -1074,7 +1074,8 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, 
 
 // ---------------------------------------------------------- graph step
 // The table build and the sampling without host synchronisation, for stream
-// capture: the deep passes read their item count on the device, the sample
+// capture (the phase events are recorded as external event nodes, so that
+// the replays time the phases like the ordinary calls): the deep passes read their item count on the device, the sample
 // offsets are scanned on the device, the sampling launches read their ranges
 // on the device.  Pools keep the sizes an ordinary build gave them; an
 // overflow is reported through the error word after the replay.
@@ -1082,7 +1083,7 @@ gcv_status enqueue_table_graph(gcv_ctx* c)
 {
     const bool mixed = c->opt.precision == GCV_MIXED;
     const Batch b = batch_view(c);
-    CU(cudaEventRecord(c->ev[0], c->stream));
+    CU(cudaEventRecordWithFlags(c->ev[0], c->stream, cudaEventRecordExternal));
     CU(cudaMemsetAsync(c->ctr.p, 0, C_COUNT * sizeof(unsigned long long), c->stream));
     if (c->n_seg > 0 && c->code >= 0) {
         const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 64));
@@ -1091,7 +1092,7 @@ gcv_status enqueue_table_graph(gcv_ctx* c)
     } else if (c->n_seg > 0) {
         for (const CodeRange& r : c->code_ranges) CHECK(launch_setup_list(c, r));
     }
-    CU(cudaEventRecord(c->ev[1], c->stream));
+    CU(cudaEventRecordWithFlags(c->ev[1], c->stream, cudaEventRecordExternal));
     const bool learned = c->opt.learned && c->mlp_w && c->n_seg > 0;
     if (learned) {
         CU(cudaMemsetAsync(c->starts.p, 0, (size_t)c->n_seg * sizeof(uint32_t), c->stream));
@@ -1110,7 +1111,7 @@ gcv_status enqueue_table_graph(gcv_ctx* c)
                 if (r.code != CODE_ELLIPSE) CHECK(run(c->seg_list.p + r.begin, r.end - r.begin));
         }
     }
-    CU(cudaEventRecord(c->ev[6], c->stream));
+    CU(cudaEventRecordWithFlags(c->ev[6], c->stream, cudaEventRecordExternal));
     if (c->n_seg > 0) {
         LengthParams P{};
         P.b = b;
@@ -1135,7 +1136,7 @@ gcv_status enqueue_table_graph(gcv_ctx* c)
         CU(cudaMemsetAsync(c->ctr.p + C_WORK, 0, sizeof(unsigned long long), c->stream));
         CHECK(launch_length<2>(c, c->code, Q));
     }
-    CU(cudaEventRecord(c->ev[2], c->stream));
+    CU(cudaEventRecordWithFlags(c->ev[2], c->stream, cudaEventRecordExternal));
     const int64_t tiles = (c->n_seg + SCAN_TILE - 1) / SCAN_TILE;
     if (tiles > 0) {
         CU(cudaMemsetAsync(c->scan_status.p, 0, (size_t)tiles * sizeof(int), c->stream));
@@ -1146,7 +1147,7 @@ gcv_status enqueue_table_graph(gcv_ctx* c)
         k_curve_len<<<(unsigned)std::min<int64_t>((c->n_curve + 255) / 256, 65535), 256, 0, c->stream>>>(b, table_view(c));
         CU(cudaGetLastError());
     }
-    CU(cudaEventRecord(c->ev[3], c->stream));
+    CU(cudaEventRecordWithFlags(c->ev[3], c->stream, cudaEventRecordExternal));
     return GCV_OK;
 }
 
@@ -1166,9 +1167,9 @@ gcv_status enqueue_count_scan(gcv_ctx* c, const int* counts, const int* idx, int
 gcv_status enqueue_sampling_graph(gcv_ctx* c, const int* d_counts, const double* d_pos, int is_relative, int what,
                                   double* d_out)
 {
-    CU(cudaEventRecord(c->ev[4], c->stream));
+    CU(cudaEventRecordWithFlags(c->ev[4], c->stream, cudaEventRecordExternal));
     if (c->n_curve == 0) {
-        CU(cudaEventRecord(c->ev[5], c->stream));
+        CU(cudaEventRecordWithFlags(c->ev[5], c->stream, cudaEventRecordExternal));
         return GCV_OK;
     }
     CHECK(enqueue_count_scan(c, d_counts, nullptr, c->sample_off.p));
@@ -1199,7 +1200,7 @@ gcv_status enqueue_sampling_graph(gcv_ctx* c, const int* d_counts, const double*
             CHECK(launch_sampler(c, r.code, P, nominal));
         }
     }
-    CU(cudaEventRecord(c->ev[5], c->stream));
+    CU(cudaEventRecordWithFlags(c->ev[5], c->stream, cudaEventRecordExternal));
     return GCV_OK;
 }
 
