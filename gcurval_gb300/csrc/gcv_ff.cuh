@@ -21,10 +21,31 @@ struct ff {
     float hi, lo;
 };
 
+// Dekker Fast2Sum (|a| >= |b|)
+__device__ __forceinline__ ff fast_two_sum(float a, float b);
+
+// double -> float-float from the bit pattern (integer and FP32 operations
+// only: on GB300 every FP64-pipe instruction, conversions included, costs as
+// much issue time as dozens of FP32 ones).  hi = the leading 24 significand
+// bits, lo = the remaining 29 bits scaled by 2^(e-52) (rounded to 24 bits),
+// then renormalised.  Outside 2^-100 <= |x| < 2^127 (and for 0, NaN, Inf) the
+// FP64 conversions are used.
 __device__ __forceinline__ ff ff_from_double(double x)
 {
-    const float h = __double2float_rn(x);
-    return ff{h, __double2float_rn(x - (double)h)};
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned top = (unsigned)(b >> 32);
+    const int e = (int)((top >> 20) & 0x7FFu) - 1023;
+    if (e < -100 || e > 126) {
+        const float h = __double2float_rn(x);
+        return ff{h, __double2float_rn(x - (double)h)};
+    }
+    const unsigned sign = top & 0x80000000u;
+    const unsigned long long m = b & 0xFFFFFFFFFFFFFull;  // 52 significand bits
+    const float hi = __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)(m >> 29));
+    const int sc = e - 52, s1 = sc / 2, s2 = sc - s1;   // two factors inside the float range
+    float lo = __uint2float_rn((unsigned)(m & 0x1FFFFFFFull));
+    lo = lo * __int_as_float((s1 + 127) << 23) * __int_as_float((s2 + 127) << 23);
+    return fast_two_sum(hi, sign ? -lo : lo);
 }
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }

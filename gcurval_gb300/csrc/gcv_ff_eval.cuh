@@ -215,6 +215,26 @@ __device__ void bspline_setup_ff(const double* __restrict__ kv, const double* __
 
 // float-float panel: K15, G7, right-end speed and slope of [vlo, vlo + 2 hw]
 // with vlo = -1 + k 2^(1-depth) built exactly from the integer k.
+// Kronrod nodes x0..x6, weights wk0..wk7 and Gauss weights wg0..wg7 (0 for
+// the Kronrod-only nodes) as float-float pairs, for the rolled panel loop
+#define GCV_FFC2(x) {split_const(x).hi, split_const(x).lo}
+static __constant__ float2 c_gk_ff[23] = {
+    GCV_FFC2(gk_x(0)),  GCV_FFC2(gk_x(1)),  GCV_FFC2(gk_x(2)),  GCV_FFC2(gk_x(3)),  GCV_FFC2(gk_x(4)),
+    GCV_FFC2(gk_x(5)),  GCV_FFC2(gk_x(6)),  GCV_FFC2(gk_wk(0)), GCV_FFC2(gk_wk(1)), GCV_FFC2(gk_wk(2)),
+    GCV_FFC2(gk_wk(3)), GCV_FFC2(gk_wk(4)), GCV_FFC2(gk_wk(5)), GCV_FFC2(gk_wk(6)), GCV_FFC2(gk_wk(7)),
+    GCV_FFC2(gk_wg(0)), GCV_FFC2(gk_wg(1)), GCV_FFC2(gk_wg(2)), GCV_FFC2(gk_wg(3)), GCV_FFC2(gk_wg(4)),
+    GCV_FFC2(gk_wg(5)), GCV_FFC2(gk_wg(6)), GCV_FFC2(gk_wg(7))};
+#undef GCV_FFC2
+
+// Large integrands (high degree x dimension, and the float-float ellipse with
+// its two Taylor series) keep the node loop rolled: fourteen inlined copies
+// overflow the instruction cache.
+template <int CODE>
+constexpr bool panel_rolled()
+{
+    return CODE == 0 || code_degree(CODE) * code_dim(CODE) >= 8;
+}
+
 template <int CODE>
 __device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, int depth, ff& K, ff& G, ff& fend,
                                              float& qend)
@@ -227,12 +247,22 @@ __device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, 
     const ff fc = EvalFF<CODE>::speed(r, mid);
     ff kk = ff_mul(to_ff(split_const(gk_wk(7))), fc);
     ff gg = ff_mul(to_ff(split_const(gk_wg(7))), fc);
+    if constexpr (panel_rolled<CODE>()) {
+#pragma unroll 1
+        for (int i = 0; i < 7; ++i) {
+            const ff dx = ff_scale(ff{c_gk_ff[i].x, c_gk_ff[i].y}, hw);
+            const ff s = ff_add(EvalFF<CODE>::speed(r, ff_add(mid, ff_neg(dx))), EvalFF<CODE>::speed(r, ff_add(mid, dx)));
+            kk = ff_fma(ff{c_gk_ff[7 + i].x, c_gk_ff[7 + i].y}, s, kk);
+            gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, s, gg);  // weight 0 on Kronrod-only nodes
+        }
+    } else {
 #pragma unroll
-    for (int i = 0; i < 7; ++i) {
-        const ff dx = ff_scale(to_ff(split_const(gk_x(i))), hw);
-        const ff s = ff_add(EvalFF<CODE>::speed(r, ff_add(mid, ff_neg(dx))), EvalFF<CODE>::speed(r, ff_add(mid, dx)));
-        kk = ff_fma(to_ff(split_const(gk_wk(i))), s, kk);
-        if (i & 1) gg = ff_fma(to_ff(split_const(gk_wg(i))), s, gg);
+        for (int i = 0; i < 7; ++i) {
+            const ff dx = ff_scale(to_ff(split_const(gk_x(i))), hw);
+            const ff s = ff_add(EvalFF<CODE>::speed(r, ff_add(mid, ff_neg(dx))), EvalFF<CODE>::speed(r, ff_add(mid, dx)));
+            kk = ff_fma(to_ff(split_const(gk_wk(i))), s, kk);
+            if (i & 1) gg = ff_fma(to_ff(split_const(gk_wg(i))), s, gg);
+        }
     }
     fend = EvalFF<CODE>::speed_slope(r, ff_add_f(vlo, 2.0f * hw), qend);
     K = ff_scale(kk, hw);

@@ -19,12 +19,16 @@ __device__ __forceinline__ void panel_k15(const double* r, double vlo, double hw
     const double fc = Eval<CODE>::speed(r, mid);
     double k = gk_wk(7) * fc;
     double g = gk_wg(7) * fc;
+    // unrolled: the FP64 integrands are compact (the float-float panels of
+    // large integrands keep their node loop rolled, see panel_k15_ff)
+    {
 #pragma unroll
-    for (int i = 0; i < 7; ++i) {
-        const double dx = hw * gk_x(i);
-        const double s = Eval<CODE>::speed(r, mid - dx) + Eval<CODE>::speed(r, mid + dx);
-        k = fma(gk_wk(i), s, k);
-        if (i & 1) g = fma(gk_wg(i), s, g);
+        for (int i = 0; i < 7; ++i) {
+            const double dx = hw * gk_x(i);
+            const double s = Eval<CODE>::speed(r, mid - dx) + Eval<CODE>::speed(r, mid + dx);
+            k = fma(gk_wk(i), s, k);
+            if (i & 1) g = fma(gk_wg(i), s, g);
+        }
     }
     fend = Eval<CODE>::speed_slope(r, vlo + 2.0 * hw, qend);
     K = k * hw;
