@@ -991,6 +991,7 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, 
     P.n_samples = total;
     P.collect = c->opt.collect_stats;
     P.rtol = c->opt.rtol;
+    P.eps_frac = (float)(0.01 * c->opt.rtol);
     P.curve_list = nullptr;
     P.list_off = nullptr;
     P.cb = P.ce = 0;
@@ -1007,8 +1008,15 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, 
         }
         CHECK(upload(c->list_sample_off, lo.data(), lo.size(), c->stream));
     }
+    const int width_bytes = width * (int)sizeof(double);
     if (!h_pos && !h_out) {
         CHECK(launch_sample_chunk(c, P, 0, n, lo));
+    } else if ((int64_t)total * width_bytes <= (int64_t)STAGE_CHUNK) {
+        // one chunk's worth: plain copies around the kernels
+        if (h_pos) CU(cudaMemcpyAsync(d_pos, h_pos, (size_t)total * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        CHECK(launch_sample_chunk(c, P, 0, n, lo));
+        if (h_out)
+            CU(cudaMemcpyAsync(h_out, d_out, (size_t)total * width_bytes, cudaMemcpyDeviceToHost, c->stream));
     } else {
         // chunks of whole curves of about STAGE_CHUNK bytes of positions
         const int64_t per = (int64_t)(STAGE_CHUNK / sizeof(double));
@@ -1184,6 +1192,7 @@ gcv_status enqueue_sampling_graph(gcv_ctx* c, const int* d_counts, const double*
     P.out = d_out;
     P.collect = c->opt.collect_stats;
     P.rtol = c->opt.rtol;
+    P.eps_frac = (float)(0.01 * c->opt.rtol);
     // grids for any sample count: the kernels loop over their ranges
     const int64_t nominal = (int64_t)sm_count() * c->knobs.sample_blocks_per_sm * c->knobs.sample_threads;
     if (c->code >= 0) {

@@ -94,6 +94,7 @@ struct SampleParams {
     int64_t n_samples;
     int collect;
     double rtol;  // the table's tolerance: samples are placed to 1 % of rtol * L
+    float eps_frac;  // 0.01 * rtol (the mixed sampler's stopping threshold over L)
     // Batches that mix curve codes run one launch per code over the curves
     // curve_list[cb .. ce) (grouped by code); list_off is the prefix of their
     // sample counts in that order.  curve_list NULL: all samples, curve order.

@@ -43,7 +43,7 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
     EvalFF<C>::load(seg, r);
     float blo = 0.0f, bhi = dv;
     ff w{dvg, 0.0f};
-    double wfinal = dvg;
+    float last = 0.0f;  // the converged Newton step, applied in FP64 at the end
     for (int it = 0; it < NEWTON_MAXIT; ++it) {
         ++newton;
         const bool from_left = w.hi <= 0.5f * dv;
@@ -70,10 +70,7 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
         // F = S(v) - target inside the leaf
         const ff F = from_left ? ff_add(I, ff_neg(rl)) : ff_add(ff_add(dS, ff_neg(I)), ff_neg(rl));
         const float Fh = F.hi + F.lo;
-        if (Fh == 0.0f) {
-            wfinal = (double)w.hi + (double)w.lo;
-            break;
-        }
+        if (Fh == 0.0f) break;
         if (Fh < 0.0f)
             blo = w.hi;
         else
@@ -82,8 +79,7 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
         const ff fv = EvalFF<C>::speed_slope(r, ff_add(vaf, w), qv);
         const float dn = Fh / fv.hi;
         if (0.5f * fabsf(qv) * dn * dn <= eps_s * fv.hi) {
-            // converged: the final update in FP64
-            wfinal = ((double)w.hi + (double)w.lo) - (double)dn;
+            last = dn;  // converged
             break;
         }
         const float wn = w.hi - dn;
@@ -91,9 +87,9 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
             w = ff{0.5f * (blo + bhi), 0.0f};  // safeguard (also NaN)
         else
             w = ff_add_f(w, -dn);
-        wfinal = (double)w.hi + (double)w.lo;
     }
-    return wfinal;
+    // the final update in FP64
+    return ((double)w.hi + (double)w.lo) - (double)last;
 }
 
 // Mixed-precision sampling: table lookups and the target in FP64, the
@@ -123,10 +119,13 @@ __global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample_ff(SampleParams P
             const double L = t.curve_len[c];
             const double pos = P.pos[i];
             const double target = P.is_relative ? pos * L : pos;
-            if (!(target > 0.0)) {
+            // target <= 0 / target >= L on the bit patterns (L >= 0; a negative
+            // target has a negative pattern): integer compares, off the FP64 pipe
+            const long long tb = __double_as_longlong(target), lb = __double_as_longlong(L);
+            if (tb <= 0) {
                 s = s0;
                 v = -1.0;
-            } else if (target >= L) {
+            } else if (tb >= lb) {
                 s = s1 - 1;
                 v = 1.0;
             } else {
@@ -140,8 +139,8 @@ __global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample_ff(SampleParams P
                 if (j >= cnt) j = cnt - 1;
                 const double base = j ? t.leaf_cum[lo + j - 1] : 0.0;
                 const double va = j ? t.leaf_v[lo + j - 1] : -1.0;
-                const float fa = (float)(j ? t.leaf_f[lo + j - 1] : t.seg_f0[s]);
-                const float qa = (float)(j ? t.leaf_q[lo + j - 1] : t.seg_q0[s]);
+                const float fa = j ? t.leaf_f[lo + j - 1] : (float)t.seg_f0[s];
+                const float qa = j ? t.leaf_q[lo + j - 1] : (float)t.seg_q0[s];
                 const double vb = t.leaf_v[lo + j];
                 const double cb = t.leaf_cum[lo + j];
                 const float fb = (float)t.leaf_f[lo + j];
@@ -168,7 +167,7 @@ __global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample_ff(SampleParams P
                     dvg = fminf(fmaxf(dvg, 0.0f), dv);
                 }
                 const float2* seg = coef_ff + b.coef_off[c] + (s - s0) * code_stride(code);
-                const float eps_s = (float)(0.01 * P.rtol * L);
+                const float eps_s = P.eps_frac * (float)L;
                 double wfinal;
                 if constexpr (CODE >= 0) {
                     wfinal = ff_leaf_newton<(CODE >= 0 ? CODE : 0), true>(seg, vaf, dv, rl, dS, dvg, eps_s, newton);
