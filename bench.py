@@ -222,6 +222,23 @@ def flops_per_eval(batch) -> float:
     return float(np.mean(np.where(batch.kind == 0, ell, bs)))
 
 
+# ------------------------------------------------------- multi-rank glue
+def max_over_ranks(x: float, dist, device) -> float:
+    """The maximum of x over the ranks (x itself without a process group)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: int, ms_per_step_max: float, world: int) -> float:
+    """Whole-job units/s: every rank processes its own batch of units_per_rank
+    (weak scaling), a step lasts as long as the slowest rank."""
+    return world * units_per_rank / (ms_per_step_max * 1e-3)
+
+
 def main():
     args = parse()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -303,11 +320,7 @@ def main():
             torch.cuda.synchronize()
         if dist:
             dist.barrier()
-        total_ms = float(sum(x.elapsed_time(y) for x, y in evs))
-        if dist:
-            t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total_ms = float(t.item())
+        total_ms = max_over_ranks(float(sum(x.elapsed_time(y) for x, y in evs)), dist, dev)
         st1 = calc.stats()
         r["launches"] = st1["n_launches"] - launches0
         r["leaves"] = st1["n_leaves"]
@@ -329,7 +342,7 @@ def main():
     launches = main_r["launches"]
     leaves = main_r["leaves"]
     ms_len, ms_samp, n_newton, n_panels = main_r["ms_len"], main_r["ms_samp"], main_r["n_newton"], main_r["n_panels"]
-    value = world * n_curves / (ms_per_step * 1e-3)
+    value = job_throughput(n_curves, ms_per_step, world)
     samples_per_s = world * n_samples / (ms_per_step * 1e-3)
 
     # ---- accuracy of this run on a subset (vs the oracle) --------------------
@@ -400,11 +413,7 @@ def main():
             e2e_t.append(t[-1] - t[0])
             parts.append(np.diff(t) * 1e3)
     e2e_parts = dict(zip(["create", "table", "sample", "destroy"], np.round(np.mean(parts, axis=0), 3).tolist()))
-    e2e_s = float(np.mean(e2e_t))
-    if dist:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(float(np.mean(e2e_t)), dist, dev)
     h2d = batch.nbytes() + batch.n_samples.nbytes + pos.nbytes
     d2h = h_out.nbytes
 
@@ -420,7 +429,7 @@ def main():
         acc = accuracy_vs_oracle(sub, precision, batch.rtol, model)
     plain = None
     if plain_r is not None:
-        pv = world * n_curves / (plain_r["ms_per_step"] * 1e-3)
+        pv = job_throughput(n_curves, plain_r["ms_per_step"], world)
         plain = {"value": round(pv, 3), "unit": "curves/s", "ms_per_step": round(plain_r["ms_per_step"], 4),
                  "steps": args.plain_steps, "warmup": 1, "rtol": batch.rtol,
                  "samples_per_s": round(world * n_samples / (plain_r["ms_per_step"] * 1e-3), 1),
@@ -430,7 +439,7 @@ def main():
                  "speedup_of_this_form": round(value / pv, 3)}
     gain = None
     if mixed_r is not None:
-        mv = world * n_curves / (mixed_r["ms_per_step"] * 1e-3)
+        mv = job_throughput(n_curves, mixed_r["ms_per_step"], world)
         gain = {"mixed_without_network": {"value": round(mv, 3), "unit": "curves/s",
                                           "ms_per_step": round(mixed_r["ms_per_step"], 4),
                                           "panels": float(np.mean(mixed_r["n_panels"])),
