@@ -2,7 +2,7 @@
 driver (gcurval::ArclengthCalculateCpu, compiled from the reference tree by
 oracle/Makefile into oracle/_ref/libgcv_ref.so).
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
 Each ``<case>.npz`` holds the curve batch (CurveBatch arrays), the sample
 counts and positions, and the reference's outputs: total lengths
@@ -20,8 +20,10 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
+REF_TREE = "/root/reference"
 sys.path.insert(0, ROOT)
 
+from gcurval_gb300 import bundle  # noqa: E402
 from gcurval_gb300 import datasets as ds  # noqa: E402
 from oracle.oracle import Reference, reference_available  # noqa: E402
 
@@ -57,15 +59,24 @@ def cases():
         n_knots, knots, clen, ctrl = ds._random_knot_bsplines(np.random.default_rng(seed), deg, dim, n_ctrl, 1.0)
         out[f"bspline_p{p}_d{d}"] = ds._pack(np.ones(nb), deg, dim, n_knots, knots, clen, ctrl, np.full(nb, 9),
                                              f"bspline_p{p}_d{d}", 1e-10)
+    # real data: the first 300 curves of the reference's own dataset file,
+    # read and normalised like its loader (samples/sample2_bspline/dataset_loader.h)
+    bundle_file = os.path.join(REF_TREE, "dataset", "BSpline", "Bundle_0.txt")
+    if os.path.exists(bundle_file):
+        out["bundle_0"] = bundle.load(bundle_file, n_curve=300, samples_per_curve=9)
     return out
 
 
-def main():
+def main(names=None):
+    """Regenerates every fixture, or only the named ones (the random stream
+    of the positions is the same either way)."""
     if not reference_available():
         sys.exit("the reference tree is needed to regenerate the golden fixtures")
     rng = np.random.default_rng(7)
     for name, batch in cases().items():
         pos = _positions(rng, batch.n_curve, int(batch.n_samples[0]))
+        if names and name not in names:
+            continue
         batch.positions = pos
         ref = Reference(batch)
         lengths, us = ref.run(batch.n_samples, pos, True, 0)
@@ -83,4 +94,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
