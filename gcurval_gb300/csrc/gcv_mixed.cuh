@@ -32,8 +32,8 @@ static __constant__ float2 c_gl8_ff[12] = {
     GCV_FFC(gl8_w(0)),  GCV_FFC(gl8_w(1)),  GCV_FFC(gl8_w(2)),  GCV_FFC(gl8_w(3))};
 #undef GCV_FFC
 
-// UNROLL: fixed-code kernels unroll the Gauss loop; the runtime-dispatch
-// kernel keeps it rolled so that eleven specialised bodies fit the
+// UNROLL: small integrands unroll the Gauss loop; large ones (panel_rolled)
+// and the runtime-dispatch kernel keep it rolled, so that the body fits the
 // instruction cache.
 template <int C, bool UNROLL>
 __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg, ff vaf, float dv, ff rl, ff dS,
@@ -170,7 +170,8 @@ __global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample_ff(SampleParams P
                 const float eps_s = P.eps_frac * (float)L;
                 double wfinal;
                 if constexpr (CODE >= 0) {
-                    wfinal = ff_leaf_newton<(CODE >= 0 ? CODE : 0), true>(seg, vaf, dv, rl, dS, dvg, eps_s, newton);
+                    wfinal = ff_leaf_newton<(CODE >= 0 ? CODE : 0), !panel_rolled<(CODE >= 0 ? CODE : 0)>()>(
+                        seg, vaf, dv, rl, dS, dvg, eps_s, newton);
                 } else {
                     switch (code) {
 #define GCV_CASE(C)                                                                                \
