@@ -98,3 +98,27 @@ def test_graph_captures_again_after_an_option_change(gpu_lib):
     np.testing.assert_array_equal(calc.getAllCurveArclengths(), ref_L)
     np.testing.assert_array_equal(out.cpu().numpy(), ref_u)
     calc.close()
+
+
+def test_autotuner_settles_after_three_builds(gpu_lib):
+    # a batch shape of its own (interval count) so that no earlier test tuned it
+    b = ds.uniform_bsplines(777, n_ctrl=23, degree=4, dim=3, n_samples=11, seed=8)
+    arrs, cnt, pos = _dev(b)
+    calc = g.ArclengthCalculateGpu.from_device_batch(*arrs, precision=g.GCV_MIXED)
+    out = torch.empty(pos.shape[0], dtype=torch.float64, device="cuda")
+    results = []
+    for i in range(5):
+        calc.createArclengthTable()
+        calc.arclengthReverseInto(cnt, pos, out, True, g.GCV_RETURN_US)
+        results.append(out.cpu().numpy().copy())
+        st = calc.stats()
+        assert st["tuned"] == (1 if i >= 2 else 0), (i, st)
+    for r in results[1:]:
+        np.testing.assert_array_equal(r, results[0])  # shapes change scheduling only
+    assert st["length_blocks_per_sm"] in (4, 6, 32) and st["sample_threads"] in (128, 256, 512)
+    # a second context of the same shape starts tuned
+    calc2 = g.ArclengthCalculateGpu.from_device_batch(*arrs, precision=g.GCV_MIXED)
+    calc2.createArclengthTable()
+    assert calc2.stats()["tuned"] == 1
+    calc2.close()
+    calc.close()
