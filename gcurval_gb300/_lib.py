@@ -109,9 +109,17 @@ _SIGS = {
     "gcv_mlp_trainer_step": (ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.c_int, ctypes.c_float, _P]),
     "gcv_mlp_infer": (ctypes.c_int, [_P, _P, ctypes.c_int, _P]),
     "gcv_set_learned_model": (ctypes.c_int, [_P, _P]),
+    # Bundle reader (include/gcurval_gb300_bundle.h)
+    "gcv_bundle_parse": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
+                                        ctypes.c_int64, ctypes.c_int, ctypes.c_int, _P, ctypes.POINTER(_P)]),
+    "gcv_bundle_sizes": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                                        ctypes.POINTER(ctypes.c_int64)]),
+    "gcv_bundle_fill": (ctypes.c_int, [_P, ctypes.c_int, _P, _P, _P, _P, _P, _P, _P]),
+    "gcv_bundle_destroy": (None, [_P]),
 }
 
 LEARNED_HEADER = os.path.join(os.path.dirname(HEADER), "gcurval_gb300_learned.h")
+BUNDLE_HEADER = os.path.join(os.path.dirname(HEADER), "gcurval_gb300_bundle.h")
 
 _lib = None
 

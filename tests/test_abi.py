@@ -16,13 +16,16 @@ def test_library_builds_and_exports_header_symbols():
     path = build.build()
     assert os.path.exists(path)
     lib = g.load()
-    declared = _lib.declared_symbols()
-    assert len(declared) >= 15
-    for name in declared:
-        assert hasattr(lib, name), name
+    assert len(_lib.declared_symbols()) >= 15
     out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
     exported = set(re.findall(r"\b(gcv_[a-z0-9_]+)\b", out))
-    assert set(declared) <= exported
+    for header in (_lib.HEADER, _lib.LEARNED_HEADER, _lib.BUNDLE_HEADER):
+        declared = _lib.declared_symbols(header)
+        assert declared, header
+        for name in declared:
+            assert hasattr(lib, name), name
+            assert name in _lib._SIGS, name  # every declared entry point has a ctypes signature
+        assert set(declared) <= exported, header
 
 
 def test_build_targets_sm103a_only():

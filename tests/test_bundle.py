@@ -43,3 +43,22 @@ def test_normalisation_like_the_reference_loader(tmp_path):
 def test_malformed_records_are_rejected(bad):
     with pytest.raises(ValueError):
         bundle.parse(bad)
+
+
+def test_device_number_conversion_matches_strtod(tmp_path):
+    """The GPU reader's decimal conversion (gcv_decimal.cuh, host and device
+    code) against the C library's correctly rounded strtod, on the host."""
+    import os
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not available")
+    here = os.path.dirname(os.path.abspath(__file__))
+    src = os.path.join(here, "bundle", "decimal_check.cpp")
+    inc = os.path.join(os.path.dirname(here), "gcurval_gb300", "csrc")
+    exe = str(tmp_path / "decimal_check")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", inc, src, "-o", exe], check=True)
+    r = subprocess.run([exe, "200000"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout[-2000:]
+    assert "mismatched 0" in r.stdout
