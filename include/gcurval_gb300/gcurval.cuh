@@ -22,7 +22,11 @@
 // stackless, one thread per interval) on |GetDerivative|, lengths are summed
 // per curve in double-double arithmetic by one warp per curve, and samples are
 // placed by safeguarded Newton steps on the leaf panels (8-point Gauss partial
-// integrals), as in the compiled library.
+// integrals), as in the compiled library.  When CurveTraits::CalculateFunction
+// names one of the reference's point-based rules (Polyline, Simpson,
+// Vincent-Forsey), the same walk refines with that rule on GetPoint instead,
+// and samples invert the rule on their leaf by bisection; GetDerivative is
+// then not needed.
 //
 // Differences from the reference, by design: the tolerance is relative
 // (rtol * interval length, default 1e-10 for double, 1e-5 for float) instead of
@@ -139,13 +143,96 @@ struct CurveTraitsBase {
     using CalculateFunction = void;
 };
 
-// Tags standing for the reference's CalculateFunction choices; this path
-// always integrates |GetDerivative| adaptively (Gauss-Kronrod), which is the
-// reference's GaussLegendreQuadrature choice made adaptive.
+// ------------------------------------------------------- length rules
+// The reference's point-based rules (gcurval/base/functors.inl.h:145-238):
+// the length of [begin, end] from the curve points a = C(begin),
+// m = C((begin + end) / 2) and b = C(end).  PointType must support
+// a + b, a - b, scalar * a and .norm(), as Eigen vectors do.
+enum LengthRule { RULE_GAUSS = 0, RULE_POLYLINE = 1, RULE_SIMPSON = 2, RULE_VINCENT_FORSEY = 3 };
+
+template <int RULE, typename Pt>
+GCURVAL_HD_FUNC double rule_from_points(const Pt& a, const Pt& m, const Pt& b)
+{
+    if constexpr (RULE == RULE_POLYLINE) {
+        (void)m;
+        return (double)(b - a).norm();  // the chord
+    } else if constexpr (RULE == RULE_SIMPSON) {
+        // Simpson's rule on |C'| with C' at begin, middle and end taken from
+        // the quadratic through the three points
+        return (1.0 / 6.0) * ((double)(-3.0 * a + 4.0 * m - b).norm() + 4.0 * (double)(b - a).norm() +
+                              (double)(a - 4.0 * m + 3.0 * b).norm());
+    } else {
+        // Vincent-Forsey: (4 (|a m| + |m b|) - |a b|) / 3
+        return 4.0 / 3.0 * ((double)(a - m).norm() + (double)(b - m).norm()) - 1.0 / 3.0 * (double)(b - a).norm();
+    }
+}
+
+namespace plugin_detail {
+template <int RULE, typename Dt>
+struct PointRule {
+    template <typename GetPoint, typename ParaPack>
+    GCURVAL_HD_FUNC Dt operator()(Dt begin, Dt end, const GetPoint& gp, const ParaPack& pack) const
+    {
+        const Dt mid = (begin + end) / Dt(2.0);
+        return (Dt)rule_from_points<RULE>(gp(begin, pack), gp(mid, pack), gp(end, pack));
+    }
+    template <typename GetPoint, typename ParaPack, typename SharedMem>
+    GCURVAL_HD_FUNC Dt operator()(Dt begin, Dt end, const GetPoint& gp, const ParaPack& pack, SharedMem& buf) const
+    {
+        const Dt mid = (begin + end) / Dt(2.0);
+        return (Dt)rule_from_points<RULE>(gp(begin, pack, buf), gp(mid, pack, buf), gp(end, pack, buf));
+    }
+};
+}  // namespace plugin_detail
+
+template <typename Dt>
+struct PolylineMethod : plugin_detail::PointRule<RULE_POLYLINE, Dt> {};
+template <typename Dt>
+struct SimpsonMethod : plugin_detail::PointRule<RULE_SIMPSON, Dt> {};
+template <typename Dt>
+struct VincentForseyRule : plugin_detail::PointRule<RULE_VINCENT_FORSEY, Dt> {};
+
+// CalculateFunction choices of CurveTraits (gcurval/base/functors.inl.h:
+// 318-339), named as in the reference.  GetP is the GetPoint functor for the
+// point-based rules.  GaussLegendreQuadrature (or no choice, void) integrates
+// |GetDerivative| by the adaptive Gauss-Kronrod walk; a point-based rule
+// refines each interval by halving where |L + R - P| (the two halves' rule
+// values against the whole's) exceeds the tolerance, as the reference's
+// arclengthRecursive does (gcurval/detail/cpu/arclength_calculate.h:242-279),
+// and accepts L + R.
 template <typename Dt, typename ParaPack, typename GetD>
 struct CalculateFunctionGaussLegendreQuadratureImpl {};
 
+#define GCURVAL_GB300_POINT_RULE(NAME, RULE)                                                           \
+    template <typename Dt, typename ParaPack, typename GetP>                                           \
+    struct CalculateFunction##NAME##Impl {                                                              \
+        static constexpr int rule = RULE;                                                               \
+        GCURVAL_HD_FUNC Dt operator()(Dt begin, Dt end, const ParaPack& pack) const                    \
+        {                                                                                               \
+            return NAME<Dt>{}(begin, end, GetP{}, pack);                                                \
+        }                                                                                               \
+        template <typename SharedMem>                                                                   \
+        GCURVAL_HD_FUNC Dt operator()(Dt begin, Dt end, const ParaPack& pack, SharedMem& buffer) const \
+        {                                                                                               \
+            return NAME<Dt>{}(begin, end, GetP{}, pack, buffer);                                        \
+        }                                                                                               \
+    };
+GCURVAL_GB300_POINT_RULE(PolylineMethod, RULE_POLYLINE)
+GCURVAL_GB300_POINT_RULE(SimpsonMethod, RULE_SIMPSON)
+GCURVAL_GB300_POINT_RULE(VincentForseyRule, RULE_VINCENT_FORSEY)
+#undef GCURVAL_GB300_POINT_RULE
+
 namespace plugin_detail {
+
+// the rule a CurveTraits::CalculateFunction selects
+template <typename CF, typename = void>
+struct RuleOf {
+    static constexpr int value = RULE_GAUSS;
+};
+template <typename CF>
+struct RuleOf<CF, std::void_t<decltype(CF::rule)>> {
+    static constexpr int value = CF::rule;
+};
 
 // 15-point Kronrod nodes / weights with the embedded 7-point Gauss weights
 // (the published G7-K15 pair), nodes descending from the right end.
@@ -255,6 +342,10 @@ struct Interval {
         return v <= 0.0 ? fma(v + 1.0, hw, t0) : fma(v - 1.0, hw, t1);
     }
     __device__ __forceinline__ double f(double v) const { return Calls<Traits>::speed((Dt)u_of(v), pk, smem) * hw; }
+    __device__ __forceinline__ typename Traits::PointType p(double v) const
+    {
+        return Calls<Traits>::point((Dt)u_of(v), pk, smem);
+    }
 };
 
 constexpr long long PANEL_BUDGET = 1ll << 22;
@@ -311,6 +402,84 @@ __device__ int walk(const Iv& iv, double rtol, int max_depth, double* len, doubl
     return n;
 }
 
+// Point-based rule of the sub-panel [v0, v1] of an interval, with its
+// end points already evaluated.
+template <int RULE, typename Iv, typename Pt>
+__device__ __forceinline__ double rule_between(const Iv& iv, double v0, double v1, const Pt& p0, const Pt& p1)
+{
+    if constexpr (RULE == RULE_POLYLINE) {
+        return rule_from_points<RULE>(p0, p0, p1);
+    } else {
+        return rule_from_points<RULE>(p0, iv.p(0.5 * (v0 + v1)), p1);
+    }
+}
+
+// The adaptive walk of a point-based rule: panel (k, depth) as in walk();
+// P = rule(panel), L and R = rule(halves); accepted when |L + R - P| is
+// within the tolerance (rtol times the interval's first estimate, halved per
+// level) or within the rounding noise of the chords, then contributes L + R.
+template <bool WRITE, int RULE, typename Iv>
+__device__ int walk_points(const Iv& iv, double rtol, int max_depth, double* len, double* lv, double* lc, float* lf)
+{
+    unsigned long long k = 0;
+    int depth = 0, n = 0;
+    long long panels = 0;
+    double cum = 0.0, tol = 0.0;
+    for (;;) {
+        const double hwp = ldexp(1.0, -depth);
+        const double vlo = fma((double)k, 2.0 * hwp, -1.0), vm = vlo + hwp, vhi = vlo + 2.0 * hwp;
+        const auto pa = iv.p(vlo);
+        const auto pm = iv.p(vm);
+        const auto pb = iv.p(vhi);
+        const double P = rule_between<RULE>(iv, vlo, vhi, pa, pb);
+        const double L = rule_between<RULE>(iv, vlo, vm, pa, pm);
+        const double R = rule_between<RULE>(iv, vm, vhi, pm, pb);
+        const double S = L + R;
+        if (depth == 0) tol = rtol * fabs(S);
+        ++panels;
+        const double noise = 64.0 * 2.220446049250313e-16 * (fabs(S) + (double)pa.norm() + (double)pb.norm());
+        const bool ok = fabs(S - P) <= fmax(tol * hwp, noise);
+        if (ok || depth >= max_depth || panels >= PANEL_BUDGET || !isfinite(S)) {
+            cum += S;
+            if (WRITE) {
+                lv[n] = vhi;
+                lc[n] = cum;
+                lf[n] = 0.0f;
+            }
+            ++n;
+            ++k;
+            const int tz = __ffsll((long long)k) - 1;
+            k >>= tz;
+            depth -= tz;
+            if (depth <= 0) break;
+        } else {
+            k <<= 1;
+            ++depth;
+        }
+    }
+    *len = cum;
+    return n;
+}
+
+// Local variable of the point at arc length r (0 <= r <= rule(v0, v1))
+// from v0 inside [v0, v1], by bisection of the rule's value over [v0, v],
+// to the resolution of v.
+template <int RULE, typename Iv>
+__device__ double invert_rule(const Iv& iv, double v0, double v1, double r)
+{
+    const auto p0 = iv.p(v0);
+    double lo = v0, hi = v1;
+    for (int it = 0; it < 64; ++it) {
+        const double mid = 0.5 * (lo + hi);
+        if (!(mid > lo && mid < hi)) break;
+        if (rule_between<RULE>(iv, v0, mid, p0, iv.p(mid)) < r)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
 struct Params {
     double rtol;
     int max_depth;
@@ -346,7 +515,12 @@ __global__ void k_intervals(Curve curve, int n_seg, const int* seg_curve, const 
         if (t1 > t0) {
             const Interval<Traits, Pack> iv{pk, t0, t1, 0.5 * (t1 - t0), smem};
             const long long o = WRITE ? leaf_off[s] : 0;
-            const int n = walk<WRITE>(iv, P.rtol, P.max_depth, &len, lv + o, lc + o, lf + o);
+            constexpr int rule = RuleOf<typename Traits::CalculateFunction>::value;
+            int n;
+            if constexpr (rule == RULE_GAUSS)
+                n = walk<WRITE>(iv, P.rtol, P.max_depth, &len, lv + o, lc + o, lf + o);
+            else
+                n = walk_points<WRITE, rule>(iv, P.rtol, P.max_depth, &len, lv + o, lc + o, lf + o);
             if (!WRITE) leaf_cnt[s] = n;
         } else if (WRITE) {  // empty interval: one leaf of length 0
             const long long o = leaf_off[s];
@@ -553,38 +727,47 @@ __global__ void k_sample(Curve curve, SampleArgs A, typename Traits::DataType* u
                 const Pack pk = typename Traits::ParaPackParser{}(curve, c, s - b, true);
                 const double t0 = A.seg_t0[s], t1 = A.seg_t1[s];
                 const Interval<Traits, Pack> iv{pk, t0, t1, 0.5 * (t1 - t0), smem};
-                const double fa = j ? (double)A.lf[lo + j - 1] : iv.f(-1.0), fb = (double)A.lf[lo + j];
-                const double dS = cb - base, dv = vb - va;
-                double sig = dS > 0.0 ? fmin(fmax((rr - base) / dS, 0.0), 1.0) : 0.0;
-                v = va + sig * dv;
-                if (fa > 0.1 * dS / dv && fb > 0.1 * dS / dv) {  // cubic Hermite of v(S): v' = 1/f
-                    const double s2 = sig * sig, s3 = s2 * sig;
-                    const double h00 = 2.0 * s3 - 3.0 * s2 + 1.0, h10 = s3 - 2.0 * s2 + sig;
-                    const double h01 = -2.0 * s3 + 3.0 * s2, h11 = s3 - s2;
-                    v = fmin(fmax(h00 * va + h01 * vb + dS * (h10 / fa + h11 / fb), va), vb);
-                }
-                const double eps = 0.01 * A.rtol * L;
-                double blo = va, bhi = vb;
-                for (int it = 0; it < 16; ++it) {
-                    const bool left = (v - va) <= (vb - v);
-                    const double a0 = left ? va : v, a1 = left ? v : vb;
-                    const double h2 = 0.5 * (a1 - a0), m2 = a0 + h2;
-                    double I = 0.0;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const double xq = h2 * gl8_x(q);
-                        I = fma(gl8_w(q), iv.f(m2 - xq) + iv.f(m2 + xq), I);
+                constexpr int rule = RuleOf<typename Traits::CalculateFunction>::value;
+                if constexpr (rule != RULE_GAUSS) {
+                    // the leaf's value is L + R of its halves: find the half,
+                    // then invert the rule on it
+                    const double vm = 0.5 * (va + vb), r = fmin(fmax(rr - base, 0.0), cb - base);
+                    const double Lh = rule_between<rule>(iv, va, vm, iv.p(va), iv.p(vm));
+                    v = r <= Lh ? invert_rule<rule>(iv, va, vm, r) : invert_rule<rule>(iv, vm, vb, r - Lh);
+                } else {
+                    const double fa = j ? (double)A.lf[lo + j - 1] : iv.f(-1.0), fb = (double)A.lf[lo + j];
+                    const double dS = cb - base, dv = vb - va;
+                    double sig = dS > 0.0 ? fmin(fmax((rr - base) / dS, 0.0), 1.0) : 0.0;
+                    v = va + sig * dv;
+                    if (fa > 0.1 * dS / dv && fb > 0.1 * dS / dv) {  // cubic Hermite of v(S): v' = 1/f
+                        const double s2 = sig * sig, s3 = s2 * sig;
+                        const double h00 = 2.0 * s3 - 3.0 * s2 + 1.0, h10 = s3 - 2.0 * s2 + sig;
+                        const double h01 = -2.0 * s3 + 3.0 * s2, h11 = s3 - s2;
+                        v = fmin(fmax(h00 * va + h01 * vb + dS * (h10 / fa + h11 / fb), va), vb);
                     }
-                    const double F = (left ? base + I * h2 : cb - I * h2) - rr;
-                    if (fabs(F) <= eps) break;
-                    if (F < 0.0)
-                        blo = v;
-                    else
-                        bhi = v;
-                    const double fv = iv.f(v);
-                    double vn = fv > 0.0 ? v - F / fv : 0.5 * (blo + bhi);
-                    if (!(vn > blo && vn < bhi)) vn = 0.5 * (blo + bhi);
-                    v = vn;
+                    const double eps = 0.01 * A.rtol * L;
+                    double blo = va, bhi = vb;
+                    for (int it = 0; it < 16; ++it) {
+                        const bool left = (v - va) <= (vb - v);
+                        const double a0 = left ? va : v, a1 = left ? v : vb;
+                        const double h2 = 0.5 * (a1 - a0), m2 = a0 + h2;
+                        double I = 0.0;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const double xq = h2 * gl8_x(q);
+                            I = fma(gl8_w(q), iv.f(m2 - xq) + iv.f(m2 + xq), I);
+                        }
+                        const double F = (left ? base + I * h2 : cb - I * h2) - rr;
+                        if (fabs(F) <= eps) break;
+                        if (F < 0.0)
+                            blo = v;
+                        else
+                            bhi = v;
+                        const double fv = iv.f(v);
+                        double vn = fv > 0.0 ? v - F / fv : 0.5 * (blo + bhi);
+                        if (!(vn > blo && vn < bhi)) vn = 0.5 * (blo + bhi);
+                        v = vn;
+                    }
                 }
             }
             const double t0 = A.seg_t0[s], t1 = A.seg_t1[s], hw = 0.5 * (t1 - t0);

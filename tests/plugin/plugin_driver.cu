@@ -1,10 +1,13 @@
 // Test driver of the header-only plugin path (include/gcurval_gb300/gcurval.cuh):
 // two user-defined curve families written the way a reference user writes
 // them (samples/sample1_ellipse/ellipse.h, samples/sample2_bspline/structs.h),
-// one of them through the shared-memory auxiliary-space hook.
+// one of them through the shared-memory auxiliary-space hook, each with the
+// default length rule (Gauss-Kronrod on GetDerivative) and with the
+// reference's point-based rules (CalculateFunction = Polyline, Simpson or
+// Vincent-Forsey on GetPoint, no GetDerivative).
 //
-//   plugin_driver ellipse <in.bin> <out.bin>
-//   plugin_driver bspline <in.bin> <out.bin>
+//   plugin_driver ellipse[_polyline|_simpson|_vf] <in.bin> <out.bin> [rtol]
+//   plugin_driver bspline[_polyline|_simpson|_vf] <in.bin> <out.bin> [rtol]
 //
 // in.bin:  int32 n_curve, int32 what (0 parameters, 1 points), then
 //          ellipse: a[n], b[n] (double);  bspline (cubic, 2D): knots_offset[n+1]
@@ -24,6 +27,9 @@ struct Vec2 {
     double x, y;
     __host__ __device__ double norm() const { return sqrt(x * x + y * y); }
 };
+__host__ __device__ inline Vec2 operator+(Vec2 a, Vec2 b) { return Vec2{a.x + b.x, a.y + b.y}; }
+__host__ __device__ inline Vec2 operator-(Vec2 a, Vec2 b) { return Vec2{a.x - b.x, a.y - b.y}; }
+__host__ __device__ inline Vec2 operator*(double s, Vec2 a) { return Vec2{s * a.x, s * a.y}; }
 
 // ------------------------------------------------------------- ellipses
 struct CurvesEllipse : g::CurvesBase<double, Vec2> {
@@ -58,19 +64,28 @@ struct TraitsEllipse : g::CurveTraitsBase<CurvesEllipse> {
     using GetPoint = PointEllipse;
     using GetDerivative = DerivEllipse;
 };
-class CalcEllipse : public g::ArclengthCalculateGpu<CurvesEllipse, TraitsEllipse> {
+// a point-based rule on GetPoint alone
+template <typename Rule>
+struct TraitsEllipseRule : g::CurveTraitsBase<CurvesEllipse> {
+    using ParaPack = PackEllipse;
+    using ParaPackParser = ParserEllipse;
+    using GetPoint = PointEllipse;
+    using CalculateFunction = Rule;
+};
+template <typename Traits>
+class CalcEllipse : public g::ArclengthCalculateGpu<CurvesEllipse, Traits> {
 public:
-    CalcEllipse(int n, const double* a, const double* b) : g::ArclengthCalculateGpu<CurvesEllipse, TraitsEllipse>(n, n)
+    CalcEllipse(int n, const double* a, const double* b) : g::ArclengthCalculateGpu<CurvesEllipse, Traits>(n, n)
     {
-        cudaMalloc(&d_curve.a, sizeof(double) * (n ? n : 1));
-        cudaMalloc(&d_curve.b, sizeof(double) * (n ? n : 1));
-        cudaMemcpy(d_curve.a, a, sizeof(double) * n, cudaMemcpyHostToDevice);
-        cudaMemcpy(d_curve.b, b, sizeof(double) * n, cudaMemcpyHostToDevice);
+        cudaMalloc(&this->d_curve.a, sizeof(double) * (n ? n : 1));
+        cudaMalloc(&this->d_curve.b, sizeof(double) * (n ? n : 1));
+        cudaMemcpy(this->d_curve.a, a, sizeof(double) * n, cudaMemcpyHostToDevice);
+        cudaMemcpy(this->d_curve.b, b, sizeof(double) * n, cudaMemcpyHostToDevice);
     }
     ~CalcEllipse() override
     {
-        cudaFree(d_curve.a);
-        cudaFree(d_curve.b);
+        cudaFree(this->d_curve.a);
+        cudaFree(this->d_curve.b);
     }
 };
 
@@ -177,24 +192,34 @@ struct TraitsBSpline : g::CurveTraitsBase<CurvesBSpline> {
     using GetPoint = PointBSpline;
     using GetDerivative = DerivBSpline;
 };
-class CalcBSpline : public g::ArclengthCalculateGpu<CurvesBSpline, TraitsBSpline> {
+template <typename Rule>
+struct TraitsBSplineRule : g::CurveTraitsBase<CurvesBSpline> {
+    using ParaPack = PackBSpline;
+    using ParaPackParser = ParserBSpline;
+    using SharedMemAllocator = ScratchAllocator;
+    using CurveLocator = LocatorBSpline;
+    using GetPoint = PointBSpline;
+    using CalculateFunction = Rule;
+};
+template <typename Traits>
+class CalcBSpline : public g::ArclengthCalculateGpu<CurvesBSpline, Traits> {
 public:
     CalcBSpline(int n, const int* ko, const double* kv, const Vec2* cp)
-        : g::ArclengthCalculateGpu<CurvesBSpline, TraitsBSpline>(n, ko[n] - (2 * P + 1) * n)
+        : g::ArclengthCalculateGpu<CurvesBSpline, Traits>(n, ko[n] - (2 * P + 1) * n)
     {
         const int nk = ko[n], np = ko[n] - (P + 1) * n;
-        cudaMalloc(&d_curve.knots_offset, sizeof(int) * (n + 1));
-        cudaMalloc(&d_curve.knot_vector, sizeof(double) * (nk ? nk : 1));
-        cudaMalloc(&d_curve.ctrl_ptrs, sizeof(Vec2) * (np ? np : 1));
-        cudaMemcpy(d_curve.knots_offset, ko, sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
-        cudaMemcpy(d_curve.knot_vector, kv, sizeof(double) * nk, cudaMemcpyHostToDevice);
-        cudaMemcpy(d_curve.ctrl_ptrs, cp, sizeof(Vec2) * np, cudaMemcpyHostToDevice);
+        cudaMalloc(&this->d_curve.knots_offset, sizeof(int) * (n + 1));
+        cudaMalloc(&this->d_curve.knot_vector, sizeof(double) * (nk ? nk : 1));
+        cudaMalloc(&this->d_curve.ctrl_ptrs, sizeof(Vec2) * (np ? np : 1));
+        cudaMemcpy(this->d_curve.knots_offset, ko, sizeof(int) * (n + 1), cudaMemcpyHostToDevice);
+        cudaMemcpy(this->d_curve.knot_vector, kv, sizeof(double) * nk, cudaMemcpyHostToDevice);
+        cudaMemcpy(this->d_curve.ctrl_ptrs, cp, sizeof(Vec2) * np, cudaMemcpyHostToDevice);
     }
     ~CalcBSpline() override
     {
-        cudaFree(d_curve.knots_offset);
-        cudaFree(d_curve.knot_vector);
-        cudaFree(d_curve.ctrl_ptrs);
+        cudaFree(this->d_curve.knots_offset);
+        cudaFree(this->d_curve.knot_vector);
+        cudaFree(this->d_curve.ctrl_ptrs);
     }
 };
 
@@ -211,8 +236,9 @@ static std::vector<T> rd(FILE* f, size_t n)
 }
 
 template <typename Calc>
-static void run(Calc& calc, int n, FILE* in, FILE* out, int what)
+static void run(Calc& calc, int n, FILE* in, FILE* out, int what, double rtol)
 {
+    if (rtol > 0.0) calc.setTolerance(rtol);
     calc.createArclengthTable();
     double* L = calc.getAllCurveArclengths();
     fwrite(L, sizeof(double), n, out);
@@ -234,28 +260,65 @@ static void run(Calc& calc, int n, FILE* in, FILE* out, int what)
     }
 }
 
+template <typename Traits>
+static void run_ellipse(int n, FILE* in, FILE* out, int what, double rtol)
+{
+    std::vector<double> a = rd<double>(in, (size_t)n), b = rd<double>(in, (size_t)n);
+    CalcEllipse<Traits> calc(n, a.data(), b.data());
+    run(calc, n, in, out, what, rtol);
+}
+
+template <typename Traits>
+static void run_bspline(int n, FILE* in, FILE* out, int what, double rtol)
+{
+    std::vector<int> ko = rd<int>(in, (size_t)n + 1);
+    std::vector<double> kv = rd<double>(in, (size_t)ko[n]);
+    std::vector<double> cp = rd<double>(in, (size_t)(ko[n] - (P + 1) * n) * 2);
+    CalcBSpline<Traits> calc(n, ko.data(), kv.data(), (const Vec2*)cp.data());
+    run(calc, n, in, out, what, rtol);
+}
+
 int main(int argc, char** argv)
 {
-    if (argc != 4) {
-        fprintf(stderr, "usage: plugin_driver ellipse|bspline in.bin out.bin\n");
+    if (argc != 4 && argc != 5) {
+        fprintf(stderr, "usage: plugin_driver ellipse|bspline[_polyline|_simpson|_vf] in.bin out.bin [rtol]\n");
         return 2;
     }
     FILE* in = fopen(argv[2], "rb");
     FILE* out = fopen(argv[3], "wb");
     if (!in || !out) return 2;
+    const double rtol = argc == 5 ? atof(argv[4]) : 0.0;
     const int n = rd<int>(in, 1)[0];
     const int what = rd<int>(in, 1)[0];
+    const std::string fam = argv[1];
+    using EP = PackEllipse;
+    using BP = PackBSpline;
     try {
-        if (std::string(argv[1]) == "ellipse") {
-            std::vector<double> a = rd<double>(in, (size_t)n), b = rd<double>(in, (size_t)n);
-            CalcEllipse calc(n, a.data(), b.data());
-            run(calc, n, in, out, what);
-        } else {
-            std::vector<int> ko = rd<int>(in, (size_t)n + 1);
-            std::vector<double> kv = rd<double>(in, (size_t)ko[n]);
-            std::vector<double> cp = rd<double>(in, (size_t)(ko[n] - (P + 1) * n) * 2);
-            CalcBSpline calc(n, ko.data(), kv.data(), (const Vec2*)cp.data());
-            run(calc, n, in, out, what);
+        if (fam == "ellipse")
+            run_ellipse<TraitsEllipse>(n, in, out, what, rtol);
+        else if (fam == "ellipse_polyline")
+            run_ellipse<TraitsEllipseRule<g::CalculateFunctionPolylineMethodImpl<double, EP, PointEllipse>>>(
+                n, in, out, what, rtol);
+        else if (fam == "ellipse_simpson")
+            run_ellipse<TraitsEllipseRule<g::CalculateFunctionSimpsonMethodImpl<double, EP, PointEllipse>>>(
+                n, in, out, what, rtol);
+        else if (fam == "ellipse_vf")
+            run_ellipse<TraitsEllipseRule<g::CalculateFunctionVincentForseyRuleImpl<double, EP, PointEllipse>>>(
+                n, in, out, what, rtol);
+        else if (fam == "bspline")
+            run_bspline<TraitsBSpline>(n, in, out, what, rtol);
+        else if (fam == "bspline_polyline")
+            run_bspline<TraitsBSplineRule<g::CalculateFunctionPolylineMethodImpl<double, BP, PointBSpline>>>(
+                n, in, out, what, rtol);
+        else if (fam == "bspline_simpson")
+            run_bspline<TraitsBSplineRule<g::CalculateFunctionSimpsonMethodImpl<double, BP, PointBSpline>>>(
+                n, in, out, what, rtol);
+        else if (fam == "bspline_vf")
+            run_bspline<TraitsBSplineRule<g::CalculateFunctionVincentForseyRuleImpl<double, BP, PointBSpline>>>(
+                n, in, out, what, rtol);
+        else {
+            fprintf(stderr, "unknown family %s\n", argv[1]);
+            return 2;
         }
     } catch (const std::exception& e) {
         fprintf(stderr, "%s\n", e.what());

@@ -1,7 +1,9 @@
 """The header-only plugin path (include/gcurval_gb300/gcurval.cuh): user-defined
 curve families through the reference's ArclengthCalculateGpu<Curve, CurveTraits>
 API, built by nvcc from tests/plugin/plugin_driver.cu and checked against the
-oracle (lengths, sample positions, points)."""
+oracle (lengths, sample positions, points), with the default Gauss-Kronrod
+rule and with the reference's point-based rules (Polyline, Simpson,
+Vincent-Forsey) selected through CurveTraits::CalculateFunction."""
 import os
 import shutil
 import subprocess
@@ -11,6 +13,7 @@ import pytest
 
 from gcurval_gb300 import datasets as ds
 from oracle import oracle as orc
+from oracle import point_rules as pr
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 pytestmark = pytest.mark.gpu
@@ -27,13 +30,14 @@ def driver(tmp_path_factory):
     return exe
 
 
-def run(driver, tmp_path, family, payload, n, total, what):
+def run(driver, tmp_path, family, payload, n, total, what, rtol=None):
     fin, fout = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
     with open(fin, "wb") as f:
         f.write(np.array([n, what], np.int32).tobytes())
         for a in payload:
             f.write(np.ascontiguousarray(a).tobytes())
-    r = subprocess.run([driver, family, fin, fout], capture_output=True, text=True, timeout=300)
+    args = [driver, family, fin, fout] + ([repr(rtol)] if rtol is not None else [])
+    r = subprocess.run(args, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     out = np.fromfile(fout, np.float64)
     L = out[:n]
@@ -111,3 +115,66 @@ def test_plugin_bsplines_through_shared_memory_hook(driver, tmp_path, maker):
     cid = np.repeat(np.arange(b.n_curve), b.n_samples)
     for i in range(0, b.total_samples, max(1, b.total_samples // 60)):
         np.testing.assert_allclose(pts[i], o.point(int(cid[i]), float(u[i]))[:2], rtol=1e-12, atol=1e-12)
+
+
+# ---------------------------------------------------------- point-based rules
+RULES = {"polyline": pr.POLYLINE, "simpson": pr.SIMPSON, "vf": pr.VINCENT_FORSEY}
+# the polyline converges at third order only: a looser tolerance keeps its tables small
+RULE_RTOL = {"polyline": 1e-6, "simpson": 1e-9, "vf": 1e-10}
+
+
+@pytest.mark.parametrize("rule", sorted(RULES))
+def test_plugin_point_rules_ellipses(driver, tmp_path, rule):
+    b = ds.ellipses(60, n_samples=17, seed=9)
+    b.sample_positions()
+    rtol = RULE_RTOL[rule]
+    L, u = run(driver, tmp_path, "ellipse_" + rule, ellipse_payload(b), b.n_curve, b.total_samples, 0, rtol)
+    o = orc.Oracle(b)
+    Lo = o.lengths()
+    assert np.max(np.abs(L - Lo) / Lo) <= 2 * rtol
+    assert sample_err(o, b, u, Lo) <= 3 * rtol
+
+
+@pytest.mark.parametrize("rule", sorted(RULES))
+def test_plugin_point_rules_bsplines_through_shared_memory_hook(driver, tmp_path, rule):
+    b = ragged_cubic_2d(80, 12)
+    b.sample_positions()
+    rtol = RULE_RTOL[rule]
+    L, u = run(driver, tmp_path, "bspline_" + rule, bspline_payload(b), b.n_curve, b.total_samples, 0, rtol)
+    o = orc.Oracle(b)
+    Lo = o.lengths()
+    assert np.max(np.abs(L - Lo) / Lo) <= 2 * rtol
+    assert sample_err(o, b, u, Lo) <= 3 * rtol
+    _, pts = run(driver, tmp_path, "bspline_" + rule, bspline_payload(b), b.n_curve, b.total_samples, 1, rtol)
+    cid = np.repeat(np.arange(b.n_curve), b.n_samples)
+    for i in range(0, b.total_samples, max(1, b.total_samples // 40)):
+        np.testing.assert_allclose(pts[i], o.point(int(cid[i]), float(u[i]))[:2], rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("rule", sorted(RULES))
+def test_plugin_point_rule_values_match_the_oracle(driver, tmp_path, rule):
+    """With an unbounded tolerance every interval is accepted at once, so a
+    curve's length is the sum over its intervals of rule(first half) +
+    rule(second half): the rule formulas themselves, against the oracle."""
+    kind = RULES[rule]
+    e = ds.ellipses(12, n_samples=2, seed=4)
+    e.sample_positions()
+    L, _ = run(driver, tmp_path, "ellipse_" + rule, ellipse_payload(e), e.n_curve, e.total_samples, 0, 1e300)
+    prm = e.ctrl.reshape(-1, 5)
+    for c in range(e.n_curve):
+        pt = lambda t, a=prm[c, 0], bb=prm[c, 1]: np.array([a * np.cos(t), bb * np.sin(t)])
+        exp = pr.rule_on(kind, pt, 0.0, np.pi) + pr.rule_on(kind, pt, np.pi, 2 * np.pi)
+        assert L[c] == pytest.approx(exp, rel=1e-13, abs=1e-13)
+    b = ragged_cubic_2d(10, 13)
+    b.sample_positions()
+    L, _ = run(driver, tmp_path, "bspline_" + rule, bspline_payload(b), b.n_curve, b.total_samples, 0, 1e300)
+    o = orc.Oracle(b)
+    for c in range(b.n_curve):
+        kv = b.knots[b.knot_off[c]:b.knot_off[c + 1]]
+        pt = lambda t, c=c: np.asarray(o.point(c, float(t)))[:2]
+        exp = 0.0
+        for t0, t1 in zip(kv[3:-4], kv[4:-3]):
+            if t1 > t0:
+                tm = 0.5 * (t0 + t1)
+                exp += pr.rule_on(kind, pt, t0, tm) + pr.rule_on(kind, pt, tm, t1)
+        assert L[c] == pytest.approx(exp, rel=1e-12)
