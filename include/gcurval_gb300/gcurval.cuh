@@ -31,9 +31,10 @@
 // Differences from the reference, by design: the tolerance is relative
 // (rtol * interval length, default 1e-10 for double, 1e-5 for float) instead of
 // the fixed absolute per-level epsilon (gcurval/base/constants.inl.h:8-70);
-// n_subdivided only sets the depth limit (max_recursive_depth + log2
-// n_subdivided levels below the interval, the reference's finest
-// resolution) because the walk starts at the whole interval; CUDA errors
+// n_subdivided sets the depth limit (max_recursive_depth + log2 n_subdivided
+// levels below the interval, the reference's finest resolution); the Gauss-
+// Kronrod walk starts at the whole interval, the point-based rules at
+// n_subdivided equal pieces as the reference's table does; CUDA errors
 // throw std::runtime_error instead of printing and exiting
 // (gcurval/detail/cuda/util.h:14-34).  Internal sums run in double for either
 // DataType.
@@ -418,8 +419,14 @@ __device__ __forceinline__ double rule_between(const Iv& iv, double v0, double v
 // P = rule(panel), L and R = rule(halves); accepted when |L + R - P| is
 // within the tolerance (rtol times the interval's first estimate, halved per
 // level) or within the rounding noise of the chords, then contributes L + R.
+// Panels above min_depth are always split: the walk starts from 2^min_depth
+// equal pieces, as the reference's table starts from n_subdivided pieces per
+// interval (gcurval/detail/cuda/kernel/generic.inl.cuh:10-48), because three
+// or five points of a whole interval can agree by accident (an S-shaped
+// interval whose quarter points line up).
 template <bool WRITE, int RULE, typename Iv>
-__device__ int walk_points(const Iv& iv, double rtol, int max_depth, double* len, double* lv, double* lc, float* lf)
+__device__ int walk_points(const Iv& iv, double rtol, int min_depth, int max_depth, double* len, double* lv, double* lc,
+                           float* lf)
 {
     unsigned long long k = 0;
     int depth = 0, n = 0;
@@ -438,7 +445,7 @@ __device__ int walk_points(const Iv& iv, double rtol, int max_depth, double* len
         if (depth == 0) tol = rtol * fabs(S);
         ++panels;
         const double noise = 64.0 * 2.220446049250313e-16 * (fabs(S) + (double)pa.norm() + (double)pb.norm());
-        const bool ok = fabs(S - P) <= fmax(tol * hwp, noise);
+        const bool ok = depth >= min_depth && fabs(S - P) <= fmax(tol * hwp, noise);
         if (ok || depth >= max_depth || panels >= PANEL_BUDGET || !isfinite(S)) {
             cum += S;
             if (WRITE) {
@@ -483,6 +490,7 @@ __device__ double invert_rule(const Iv& iv, double v0, double v1, double r)
 struct Params {
     double rtol;
     int max_depth;
+    int min_depth;  // point-based rules: log2(n_subdivided)
 };
 
 // curve -> its interval range (CurveLocator), interval -> (curve, local id)
@@ -520,7 +528,7 @@ __global__ void k_intervals(Curve curve, int n_seg, const int* seg_curve, const 
             if constexpr (rule == RULE_GAUSS)
                 n = walk<WRITE>(iv, P.rtol, P.max_depth, &len, lv + o, lc + o, lf + o);
             else
-                n = walk_points<WRITE, rule>(iv, P.rtol, P.max_depth, &len, lv + o, lc + o, lf + o);
+                n = walk_points<WRITE, rule>(iv, P.rtol, P.min_depth, P.max_depth, &len, lv + o, lc + o, lf + o);
             if (!WRITE) leaf_cnt[s] = n;
         } else if (WRITE) {  // empty interval: one leaf of length 0
             const long long o = leaf_off[s];
@@ -846,7 +854,7 @@ public:
                                                                                curve_b.p, curve_e.p);
             check(cudaGetLastError(), "k_locate");
         }
-        Params P{rtol, max_recursive_depth + ilog2(n_subdivided)};
+        Params P{rtol, max_recursive_depth + ilog2(n_subdivided), ilog2(n_subdivided)};
         if (n_seg > 0) {
             k_intervals<false, Curve, CurveTraits><<<grid(n_seg), kThreads, smem, stream>>>(
                 d_curve, n_seg, seg_curve.p, seg_sid.p, P, leaf_cnt.p, seg_len.p, seg_t0.p, seg_t1.p, nullptr, nullptr,
