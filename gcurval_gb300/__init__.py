@@ -24,10 +24,11 @@ import ctypes
 import numpy as np
 
 from ._lib import (GCV_DEVICE, GCV_HOST, GCV_MIXED, GCV_PLAIN_FP64, GCV_RETURN_POINTS, GCV_RETURN_US,
-                   GcvError, Options, Result, Stats, check, default_options, load)
+                   GcvError, Options, Result, Stats, check, default_options, load, release_cached_memory)
 
 __all__ = ["ArclengthCalculateGpu", "ArclengthReverseResult", "GcvError", "GCV_DEVICE", "GCV_HOST",
-           "GCV_RETURN_US", "GCV_RETURN_POINTS", "GCV_PLAIN_FP64", "GCV_MIXED", "default_options", "load"]
+           "GCV_RETURN_US", "GCV_RETURN_POINTS", "GCV_PLAIN_FP64", "GCV_MIXED", "default_options", "load",
+           "release_cached_memory"]
 
 _P = ctypes.c_void_p
 

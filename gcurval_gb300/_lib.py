@@ -91,6 +91,7 @@ _SIGS = {
     "gcv_get_shape": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                                      ctypes.POINTER(ctypes.c_int)]),
     "gcv_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    "gcv_release_cached_memory": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
     "gcv_step_graph": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, _P]),
     "gcv_step_graph_reset": (ctypes.c_int, [_P]),
     "gcv_bspline_lengths_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
@@ -155,6 +156,15 @@ def check(status: int) -> None:
     if status != GCV_OK:
         msg = _lib.gcv_last_error().decode() if _lib is not None else ""
         raise GcvError(status, msg)
+
+
+def release_cached_memory() -> int:
+    """Frees the device buffers destroyed contexts left in the library's
+    memory cache; returns the bytes freed."""
+    lib = load()
+    n = ctypes.c_int64()
+    check(lib.gcv_release_cached_memory(ctypes.byref(n)))
+    return n.value
 
 
 def measure_fma_peak(which: int) -> float:

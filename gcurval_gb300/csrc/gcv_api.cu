@@ -57,10 +57,108 @@ gcv_status cuda_fail(cudaError_t e, const char* what)
         if (s_ != GCV_OK) return s_;                                                               \
     } while (0)
 
+// ---------------------------------------------------- device memory cache
+// A destroyed context hands its device buffers to a process-wide cache, and
+// the next context that asks for a similar size (at most 1/8 larger) takes
+// one from there instead of calling cudaMalloc: the counterpart of the
+// memory pool the reference's samples can start (RMM,
+// samples/sample1_ellipse/main.cpp:147-155).  Creating and destroying
+// contexts of one batch shape then maps and unmaps none of the ~100 GB a
+// 1M-curve table holds.  Buffers enter the cache only after a device-wide
+// synchronisation (what cudaFree would have done), so a cached block is idle.
+// A cudaMalloc that runs out of memory frees the cache and tries again.
+// GCV_NO_MEMORY_CACHE=1 in the environment turns the cache off;
+// gcv_release_cached_memory() frees it.
+struct CachedBlock {
+    void* p;
+    int dev;
+};
+std::mutex g_cache_m;
+std::multimap<size_t, CachedBlock> g_cache;  // by size in bytes
+
+bool cache_enabled()
+{
+    static const bool on = [] {
+        const char* v = std::getenv("GCV_NO_MEMORY_CACHE");
+        return !(v && v[0] && v[0] != '0');
+    }();
+    return on;
+}
+
+int current_device()
+{
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev;
+}
+
+// frees the cached blocks of device `dev` (-1: of every device); returns bytes
+size_t release_cache(int dev)
+{
+    std::vector<std::pair<void*, int>> drop;
+    size_t bytes = 0;
+    {
+        std::lock_guard<std::mutex> g(g_cache_m);
+        for (auto it = g_cache.begin(); it != g_cache.end();) {
+            if (dev < 0 || it->second.dev == dev) {
+                drop.push_back({it->second.p, it->second.dev});
+                bytes += it->first;
+                it = g_cache.erase(it);
+            } else {
+                ++it;
+            }
+        }
+    }
+    const int cur = current_device();
+    for (auto& d : drop) {
+        if (d.second != cur) cudaSetDevice(d.second);
+        cudaFree(d.first);
+        if (d.second != cur) cudaSetDevice(cur);
+    }
+    return bytes;
+}
+
+// a block of at least `bytes`; *got = its size
+cudaError_t dev_alloc(void** p, size_t bytes, size_t* got)
+{
+    const int dev = current_device();
+    if (cache_enabled()) {
+        std::lock_guard<std::mutex> g(g_cache_m);
+        for (auto it = g_cache.lower_bound(bytes); it != g_cache.end() && it->first <= bytes + bytes / 8; ++it) {
+            if (it->second.dev == dev) {
+                *p = it->second.p;
+                *got = it->first;
+                g_cache.erase(it);
+                return cudaSuccess;
+            }
+        }
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation && cache_enabled()) {
+        cudaGetLastError();
+        if (release_cache(dev) > 0) e = cudaMalloc(p, bytes);
+    }
+    *got = e == cudaSuccess ? bytes : 0;
+    return e;
+}
+
+// an idle block into the cache (or freed when the cache is off)
+void dev_recycle(void* p, size_t bytes)
+{
+    if (!p) return;
+    if (!cache_enabled()) {
+        cudaFree(p);
+        return;
+    }
+    std::lock_guard<std::mutex> g(g_cache_m);
+    g_cache.insert({bytes, CachedBlock{p, current_device()}});
+}
+
 template <typename T>
 struct DBuf {
     T* p = nullptr;
     size_t n = 0;
+    size_t bytes = 0;  // size of the block behind p (owned blocks)
     bool owned = true;
 
     gcv_status reserve(size_t count)
@@ -68,13 +166,18 @@ struct DBuf {
         if (count <= n && p) return GCV_OK;
         release();
         if (count == 0) count = 1;
-        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        void* q = nullptr;
+        size_t got = 0;
+        cudaError_t e = dev_alloc(&q, count * sizeof(T), &got);
         if (e != cudaSuccess) {
             p = nullptr;
             n = 0;
+            bytes = 0;
             return cuda_fail(e, "cudaMalloc");
         }
+        p = static_cast<T*>(q);
         n = count;
+        bytes = got;
         owned = true;
         return GCV_OK;
     }
@@ -83,13 +186,26 @@ struct DBuf {
         release();
         p = const_cast<T*>(q);
         n = count;
+        bytes = 0;
         owned = false;
     }
+    // frees at once (cudaFree synchronises the device): for buffers replaced
+    // while the context's work may still be in flight
     void release()
     {
         if (p && owned) cudaFree(p);
         p = nullptr;
         n = 0;
+        bytes = 0;
+        owned = true;
+    }
+    // to the cache: only when the device is idle (context destruction)
+    void recycle()
+    {
+        if (p && owned) dev_recycle(p, bytes);
+        p = nullptr;
+        n = 0;
+        bytes = 0;
         owned = true;
     }
 };
@@ -307,47 +423,50 @@ gcv_status check_options(const gcv_options* o)
 void destroy_ctx(gcv_ctx* c)
 {
     if (!c) return;
-    c->kind.release();
-    c->degree.release();
-    c->dim.release();
-    c->knot_off.release();
-    c->ctrl_off.release();
-    c->knots.release();
-    c->ctrl.release();
-    c->seg_off.release();
-    c->coef_off.release();
-    c->seg_curve.release();
-    c->seg_list.release();
-    c->curve_list.release();
-    c->starts.release();
-    c->feat.release();
+    // the context's buffers go to the memory cache idle, as cudaFree would
+    // have left them
+    if (cache_enabled()) cudaDeviceSynchronize();
+    c->kind.recycle();
+    c->degree.recycle();
+    c->dim.recycle();
+    c->knot_off.recycle();
+    c->ctrl_off.recycle();
+    c->knots.recycle();
+    c->ctrl.recycle();
+    c->seg_off.recycle();
+    c->coef_off.recycle();
+    c->seg_curve.recycle();
+    c->seg_list.recycle();
+    c->curve_list.recycle();
+    c->starts.recycle();
+    c->feat.recycle();
     if (c->mlp_w) cudaFree(c->mlp_w);
-    c->list_sample_off.release();
-    c->coef.release();
-    c->seg_t0.release();
-    c->seg_t1.release();
-    c->seg_f0.release();
-    c->seg_q0.release();
-    c->seg_len.release();
-    c->seg_cum.release();
-    c->curve_len.release();
-    c->leaf_off.release();
-    c->leaf_cnt.release();
-    c->leaf_v.release();
-    c->leaf_cum.release();
-    c->leaf_f.release();
-    c->leaf_q.release();
-    c->deep_list.release();
-    c->ctr.release();
-    c->scan_status.release();
-    c->scan_flag.release();
-    c->scan_hi.release();
-    c->scan_lo.release();
-    c->sample_off.release();
-    c->sample_cnt.release();
-    c->sample_pos.release();
-    c->sample_out.release();
-    c->coef_ff.release();
+    c->list_sample_off.recycle();
+    c->coef.recycle();
+    c->seg_t0.recycle();
+    c->seg_t1.recycle();
+    c->seg_f0.recycle();
+    c->seg_q0.recycle();
+    c->seg_len.recycle();
+    c->seg_cum.recycle();
+    c->curve_len.recycle();
+    c->leaf_off.recycle();
+    c->leaf_cnt.recycle();
+    c->leaf_v.recycle();
+    c->leaf_cum.recycle();
+    c->leaf_f.recycle();
+    c->leaf_q.recycle();
+    c->deep_list.recycle();
+    c->ctr.recycle();
+    c->scan_status.recycle();
+    c->scan_flag.recycle();
+    c->scan_hi.recycle();
+    c->scan_lo.recycle();
+    c->sample_off.recycle();
+    c->sample_cnt.recycle();
+    c->sample_pos.recycle();
+    c->sample_out.recycle();
+    c->coef_ff.recycle();
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
     for (int k = 0; k < STREAM_EVENTS; ++k) {
         if (c->ev_in[k]) cudaEventDestroy(c->ev_in[k]);
@@ -357,7 +476,7 @@ void destroy_ctx(gcv_ctx* c)
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     if (c->graph) cudaGraphDestroy(c->graph);
     if (c->gstream) cudaStreamDestroy(c->gstream);
-    c->scan_blk.release();
+    c->scan_blk.recycle();
     if (c->s_in) cudaStreamDestroy(c->s_in);
     if (c->s_out) cudaStreamDestroy(c->s_out);
     for (auto& e : c->ev)
@@ -1609,6 +1728,13 @@ gcv_status gcv_get_stats(gcv_ctx* ctx, gcv_stats* out)
     ctx->stats.sample_blocks_per_sm = ctx->knobs.sample_blocks_per_sm;
     ctx->stats.tuned = ctx->len_trial < 0 ? 1 : 0;
     *out = ctx->stats;
+    return GCV_OK;
+}
+
+gcv_status gcv_release_cached_memory(int64_t* bytes)
+{
+    const size_t n = release_cache(-1);
+    if (bytes) *bytes = (int64_t)n;
     return GCV_OK;
 }
 

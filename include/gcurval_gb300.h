@@ -237,6 +237,15 @@ gcv_status gcv_get_shape(gcv_ctx* ctx, int64_t* n_curve, int64_t* n_segments, in
  * counterpart. */
 gcv_status gcv_measure_fma_peak(int which, double* tflops);
 
+/* Device memory kept for reuse: a destroyed context's buffers stay allocated
+ * in a process-wide cache and serve the next context that needs a similar
+ * size (the counterpart of the reference samples' optional RMM pool,
+ * samples/sample1_ellipse/main.cpp:147-155).  An allocation that finds the
+ * GPU full frees the cache first.  Set GCV_NO_MEMORY_CACHE=1 in the
+ * environment to free buffers at once instead.  This call frees the cached
+ * buffers of every device; *bytes (may be NULL) receives how many bytes. */
+gcv_status gcv_release_cached_memory(int64_t* bytes);
+
 /* ---- allocation-free lengths ---------------------------------------------- */
 
 /* Largest number of knot intervals gcv_bspline_lengths_noalloc accepts. */
