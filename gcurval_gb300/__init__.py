@@ -24,7 +24,8 @@ import ctypes
 import numpy as np
 
 from ._lib import (GCV_DEVICE, GCV_HOST, GCV_MIXED, GCV_PLAIN_FP64, GCV_RETURN_POINTS, GCV_RETURN_US,
-                   GcvError, Options, Result, Stats, check, default_options, load, release_cached_memory)
+                   GcvError, Options, Result, ResultF32, Stats, check, default_options, load,
+                   release_cached_memory)
 
 __all__ = ["ArclengthCalculateGpu", "ArclengthReverseResult", "GcvError", "GCV_DEVICE", "GCV_HOST",
            "GCV_RETURN_US", "GCV_RETURN_POINTS", "GCV_PLAIN_FP64", "GCV_MIXED", "default_options", "load",
@@ -43,6 +44,12 @@ def _ptr(a):
 
 def _is_device(a) -> bool:
     return hasattr(a, "is_cuda") and bool(a.is_cuda)
+
+
+def _is_f32(a) -> bool:
+    """A float32 numpy array or torch tensor."""
+    dt = getattr(a, "dtype", None)
+    return dt is not None and str(dt) in ("float32", "torch.float32")
 
 
 _cudart_lib = None
@@ -77,9 +84,10 @@ class ArclengthReverseResult:
     parameters ``us`` or ``points`` (n_points x dim), in host memory (numpy)
     or device memory (owned by this object, freed with it)."""
 
-    def __init__(self, res: Result, lib):
+    def __init__(self, res, lib, dtype=np.float64):
         self._res = res
         self._lib = lib
+        self.dtype = np.dtype(dtype)
         self.n_points = int(res.n_points)
         self.store_where = int(res.store_where)
         self.store_what = int(res.store_what)
@@ -92,13 +100,14 @@ class ArclengthReverseResult:
     def numpy(self) -> np.ndarray:
         width = 1 if self.store_what == GCV_RETURN_US else self.point_dim
         n = self.n_points * width
-        out = np.empty(n, np.float64)
+        out = np.empty(n, self.dtype)
+        nb = n * self.dtype.itemsize
         if n:
             if self.store_where == GCV_HOST:
-                ctypes.memmove(out.ctypes.data, self._res.data, n * 8)
+                ctypes.memmove(out.ctypes.data, self._res.data, nb)
             else:
                 rc = _cudart().cudaMemcpy(ctypes.c_void_p(out.ctypes.data), ctypes.c_void_p(self._res.data),
-                                          ctypes.c_size_t(n * 8), 2)  # cudaMemcpyDeviceToHost
+                                          ctypes.c_size_t(nb), 2)  # cudaMemcpyDeviceToHost
                 if rc != 0:
                     raise GcvError(2, f"cudaMemcpy of the device result failed ({rc})")
         return out if width == 1 else out.reshape(-1, width)
@@ -113,7 +122,10 @@ class ArclengthReverseResult:
 
     def free(self):
         if self._res is not None and self._res.data:
-            self._lib.gcv_free_result(ctypes.byref(self._res))
+            if self.dtype == np.float32:
+                self._lib.gcv_free_result_f32(ctypes.byref(self._res))
+            else:
+                self._lib.gcv_free_result(ctypes.byref(self._res))
         self._res = None
 
     def __del__(self):
@@ -126,10 +138,14 @@ class ArclengthReverseResult:
 class ArclengthCalculateGpu:
     """One batch of curves on the GPU (a gcv_ctx)."""
 
-    def __init__(self, handle, keep=()):
+    def __init__(self, handle, keep=(), f32=False):
         self._lib = load()
         self._h = handle
         self._keep = keep  # host/device arrays the context borrows
+        # FP32 data (the reference's ArclengthCalculateGpu<float>): float
+        # lengths, positions, parameters and points
+        self.f32 = bool(f32)
+        self.dtype = np.float32 if f32 else np.float64
         n = ctypes.c_int64()
         s = ctypes.c_int64()
         d = ctypes.c_int()
@@ -155,29 +171,37 @@ class ArclengthCalculateGpu:
 
     @classmethod
     def ellipses(cls, a, b, rot=None, cx=None, cy=None, **kw):
-        """samples/sample1_ellipse/ellipse.h:121-129 (plus rotation and centre)."""
+        """samples/sample1_ellipse/ellipse.h:121-129 (plus rotation and centre).
+        float32 arrays select the FP32 entry points (Dt = float)."""
         lib = load()
-        arrs = [None if x is None else (x if _is_device(x) else np.ascontiguousarray(x, np.float64))
+        f32 = _is_f32(a)
+        dt = np.float32 if f32 else np.float64
+        arrs = [None if x is None else (x if _is_device(x) else np.ascontiguousarray(x, dt))
                 for x in (a, b, rot, cx, cy)]
         where = GCV_DEVICE if _is_device(arrs[0]) else GCV_HOST
         h = _P()
         o = cls._opts(**kw)
-        check(lib.gcv_create_ellipses(ctypes.byref(h), len(arrs[0]), *[_ptr(x) for x in arrs], where, ctypes.byref(o)))
-        return cls(h, keep=tuple(arrs))
+        create = lib.gcv_create_ellipses_f32 if f32 else lib.gcv_create_ellipses
+        check(create(ctypes.byref(h), len(arrs[0]), *[_ptr(x) for x in arrs], where, ctypes.byref(o)))
+        return cls(h, keep=tuple(arrs), f32=f32)
 
     @classmethod
     def bsplines(cls, degree, dim, knots_offset, knot_vector, ctrl_pts, **kw):
-        """samples/sample2_bspline/arclength_calculate.h:505-518 layout."""
+        """samples/sample2_bspline/arclength_calculate.h:505-518 layout.
+        float32 knots and control points select the FP32 entry points."""
         lib = load()
         dev = _is_device(knot_vector)
+        f32 = _is_f32(knot_vector)
+        dt = np.float32 if f32 else np.float64
         ko = knots_offset if dev else np.ascontiguousarray(knots_offset, np.int32)
-        kv = knot_vector if dev else np.ascontiguousarray(knot_vector, np.float64)
-        cp = ctrl_pts if dev else np.ascontiguousarray(ctrl_pts, np.float64)
+        kv = knot_vector if dev else np.ascontiguousarray(knot_vector, dt)
+        cp = ctrl_pts if dev else np.ascontiguousarray(ctrl_pts, dt)
         h = _P()
         o = cls._opts(**kw)
-        check(lib.gcv_create_bsplines(ctypes.byref(h), len(ko) - 1, int(degree), int(dim), _ptr(ko), _ptr(kv), _ptr(cp),
-                                      GCV_DEVICE if dev else GCV_HOST, ctypes.byref(o)))
-        return cls(h, keep=(ko, kv, cp))
+        create = lib.gcv_create_bsplines_f32 if f32 else lib.gcv_create_bsplines
+        check(create(ctypes.byref(h), len(ko) - 1, int(degree), int(dim), _ptr(ko), _ptr(kv), _ptr(cp),
+                     GCV_DEVICE if dev else GCV_HOST, ctypes.byref(o)))
+        return cls(h, keep=(ko, kv, cp), f32=f32)
 
     @classmethod
     def from_batch(cls, batch, **kw):
@@ -235,14 +259,19 @@ class ArclengthCalculateGpu:
         check(self._lib.gcv_create_arclength_table(self._h))
 
     def getAllCurveArclengths(self, out=None) -> np.ndarray:
+        get = self._lib.gcv_get_all_curve_arclengths_f32 if self.f32 else self._lib.gcv_get_all_curve_arclengths
         if out is not None and _is_device(out):
-            check(self._lib.gcv_get_all_curve_arclengths(self._h, _ptr(out), GCV_DEVICE))
+            check(get(self._h, _ptr(out), GCV_DEVICE))
             return out
-        res = np.empty(self.n_curve, np.float64)
-        check(self._lib.gcv_get_all_curve_arclengths(self._h, _ptr(res), GCV_HOST))
+        res = np.empty(self.n_curve, self.dtype)
+        check(get(self._h, _ptr(res), GCV_HOST))
         return res
 
     def getArclength(self, cid: int) -> float:
+        if self.f32:
+            v = ctypes.c_float()
+            check(self._lib.gcv_get_arclength_f32(self._h, int(cid), ctypes.byref(v)))
+            return np.float32(v.value)
         v = ctypes.c_double()
         check(self._lib.gcv_get_arclength(self._h, int(cid), ctypes.byref(v)))
         return v.value
@@ -250,12 +279,12 @@ class ArclengthCalculateGpu:
     def arclengthReverse(self, n_ptrs_for_curves, sample_position, is_relative=True, where=GCV_DEVICE,
                          what=GCV_RETURN_US) -> ArclengthReverseResult:
         n = np.ascontiguousarray(n_ptrs_for_curves, np.int32)
-        pos = np.ascontiguousarray(sample_position, np.float64)
+        pos = np.ascontiguousarray(sample_position, self.dtype)
         self._check_counts(n, pos.shape[0])
-        r = Result()
-        check(self._lib.gcv_arclength_reverse(self._h, _ptr(n), _ptr(pos), int(bool(is_relative)), int(where),
-                                              int(what), ctypes.byref(r)))
-        return ArclengthReverseResult(r, self._lib)
+        r = ResultF32() if self.f32 else Result()
+        rev = self._lib.gcv_arclength_reverse_f32 if self.f32 else self._lib.gcv_arclength_reverse
+        check(rev(self._h, _ptr(n), _ptr(pos), int(bool(is_relative)), int(where), int(what), ctypes.byref(r)))
+        return ArclengthReverseResult(r, self._lib, self.dtype)
 
     def arclengthReverseInto(self, n_ptrs_for_curves, sample_position, out, is_relative=True, what=GCV_RETURN_US):
         """Sampling into a caller buffer (numpy or torch, host or device)."""
@@ -263,15 +292,17 @@ class ArclengthCalculateGpu:
         n = n_ptrs_for_curves if _is_device(n_ptrs_for_curves) else np.ascontiguousarray(n_ptrs_for_curves, np.int32)
         if _is_device(n) != in_dev:
             raise ValueError("counts and positions must live in the same memory")
-        pos = sample_position if in_dev else np.ascontiguousarray(sample_position, np.float64)
+        pos = sample_position if in_dev else np.ascontiguousarray(sample_position, self.dtype)
+        if _is_f32(pos) != self.f32 or _is_f32(out) != self.f32:
+            raise ValueError(f"positions and output must be {np.dtype(self.dtype).name} for this context")
         total = self._check_counts(n, int(pos.shape[0]))
         width = 1 if what == GCV_RETURN_US else self.point_dim
         n_out = int(out.numel()) if hasattr(out, "numel") else int(out.size)
         if n_out < total * width:
             raise ValueError(f"output holds {n_out} values, {total * width} needed")
-        check(self._lib.gcv_arclength_reverse_into(self._h, _ptr(n), _ptr(pos), int(bool(is_relative)),
-                                                   GCV_DEVICE if in_dev else GCV_HOST, int(what), _ptr(out),
-                                                   GCV_DEVICE if _is_device(out) else GCV_HOST))
+        into = self._lib.gcv_arclength_reverse_into_f32 if self.f32 else self._lib.gcv_arclength_reverse_into
+        check(into(self._h, _ptr(n), _ptr(pos), int(bool(is_relative)), GCV_DEVICE if in_dev else GCV_HOST,
+                   int(what), _ptr(out), GCV_DEVICE if _is_device(out) else GCV_HOST))
         return out
 
     def clearArclength(self):

@@ -51,6 +51,11 @@ class Result(ctypes.Structure):
                 ("point_dim", ctypes.c_int), ("data", _P)]
 
 
+class ResultF32(ctypes.Structure):
+    _fields_ = [("n_points", ctypes.c_int64), ("store_where", ctypes.c_int), ("store_what", ctypes.c_int),
+                ("point_dim", ctypes.c_int), ("data", _P)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("n_curves", ctypes.c_int64), ("n_segments", ctypes.c_int64), ("n_leaves", ctypes.c_int64),
                 ("n_panels", ctypes.c_int64), ("n_deep_segments", ctypes.c_int64), ("n_capped", ctypes.c_int64),
@@ -94,6 +99,18 @@ _SIGS = {
     "gcv_release_cached_memory": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
     "gcv_step_graph": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, _P]),
     "gcv_step_graph_reset": (ctypes.c_int, [_P]),
+    # FP32 data
+    "gcv_create_ellipses_f32": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, _P, _P, _P, _P, _P, ctypes.c_int,
+                                               ctypes.POINTER(Options)]),
+    "gcv_create_bsplines_f32": (ctypes.c_int, [ctypes.POINTER(_P), ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P,
+                                               _P, ctypes.c_int, ctypes.POINTER(Options)]),
+    "gcv_get_all_curve_arclengths_f32": (ctypes.c_int, [_P, _P, ctypes.c_int]),
+    "gcv_get_arclength_f32": (ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]),
+    "gcv_arclength_reverse_into_f32": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P,
+                                                      ctypes.c_int]),
+    "gcv_arclength_reverse_f32": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.POINTER(ResultF32)]),
+    "gcv_free_result_f32": (ctypes.c_int, [ctypes.POINTER(ResultF32)]),
     "gcv_bspline_lengths_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
                                                    ctypes.c_double, ctypes.c_int, _P, _P]),
     # learned form (include/gcurval_gb300_learned.h)

@@ -328,6 +328,7 @@ struct gcv_ctx {
     DBuf<int64_t> sample_off;
     DBuf<int> sample_cnt;
     DBuf<double> sample_pos, sample_out;
+    DBuf<float> f32_buf;  // float positions / results of the FP32 entry points
     std::vector<int64_t> h_sample_off;
 
     std::vector<double> h_len;
@@ -466,6 +467,7 @@ void destroy_ctx(gcv_ctx* c)
     c->sample_cnt.recycle();
     c->sample_pos.recycle();
     c->sample_out.recycle();
+    c->f32_buf.recycle();
     c->coef_ff.recycle();
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
     for (int k = 0; k < STREAM_EVENTS; ++k) {
@@ -1356,6 +1358,29 @@ gcv_status stage_counts(gcv_ctx* c, const int* n_ptrs, int in_where, int64_t* to
     return GCV_OK;
 }
 
+// FP32 data: widened to double on the way in, rounded to float on the way out
+__global__ void k_widen(const float* in, double* out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = (double)in[i];
+}
+__global__ void k_narrow(const double* in, float* out, int64_t n)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = __double2float_rn(in[i]);
+}
+unsigned convert_grid(int64_t n)
+{
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, (int64_t)sm_count() * 32));
+}
+
+std::vector<double> widen_host(const float* p, size_t n)
+{
+    std::vector<double> v(n);
+    for (size_t i = 0; i < n; ++i) v[i] = (double)p[i];
+    return v;
+}
+
 }  // namespace
 
 // ===================================================================== ABI
@@ -1682,6 +1707,195 @@ gcv_status gcv_arclength_reverse(gcv_ctx* ctx, const int* n_ptrs_for_curves, con
 }
 
 gcv_status gcv_free_result(gcv_result* r)
+{
+    if (!r) return fail(GCV_ERR_INVALID, "result is NULL");
+    if (r->data) {
+        if (r->store_where == GCV_DEVICE)
+            cudaFree(r->data);
+        else
+            std::free(r->data);
+    }
+    r->data = nullptr;
+    r->n_points = 0;
+    return GCV_OK;
+}
+
+// ----------------------------------------------------------- FP32 data
+gcv_status gcv_create_ellipses_f32(gcv_ctx** out, int n_curve, const float* a, const float* b, const float* rot,
+                                   const float* cx, const float* cy, int where, const gcv_options* opt)
+{
+    if (!out) return fail(GCV_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (n_curve < 0) return fail(GCV_ERR_INVALID, "n_curve < 0");
+    if (n_curve > 0 && (!a || !b)) return fail(GCV_ERR_INVALID, "a or b is NULL");
+    const int w = where == GCV_DEVICE ? GCV_DEVICE : GCV_HOST;
+    std::vector<float> f[5];
+    const float* src[5] = {a, b, rot, cx, cy};
+    std::vector<double> d[5];
+    for (int k = 0; k < 5; ++k) {
+        if (!src[k]) continue;
+        CHECK(to_host(src[k], (size_t)n_curve, w, f[k]));
+        d[k] = widen_host(f[k].data(), f[k].size());
+    }
+    auto ptr = [&](int k) { return src[k] ? d[k].data() : nullptr; };
+    return gcv_create_ellipses(out, n_curve, ptr(0), ptr(1), ptr(2), ptr(3), ptr(4), GCV_HOST, opt);
+}
+
+gcv_status gcv_create_bsplines_f32(gcv_ctx** out, int n_curve, int degree, int dim, const int* knots_offset,
+                                   const float* knot_vector, const float* ctrl_pts, int where, const gcv_options* opt)
+{
+    if (!out) return fail(GCV_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (n_curve < 0) return fail(GCV_ERR_INVALID, "n_curve < 0");
+    if (degree < 1 || degree > MAX_DEGREE) return fail(GCV_ERR_INVALID, "degree must be in [1, 5]");
+    if (dim != 2 && dim != 3) return fail(GCV_ERR_INVALID, "dim must be 2 or 3");
+    if (!knots_offset) return fail(GCV_ERR_INVALID, "knots_offset is NULL");
+    const int w = where == GCV_DEVICE ? GCV_DEVICE : GCV_HOST;
+    std::vector<int> ko;
+    CHECK(to_host(knots_offset, (size_t)n_curve + 1, w, ko));
+    const int64_t nk = ko[(size_t)n_curve];
+    const int64_t nc = ((int64_t)ko[(size_t)n_curve] - (int64_t)(degree + 1) * n_curve) * dim;
+    if (nk < 0 || nc < 0) return fail(GCV_ERR_INVALID, "knots_offset too small for the degree");
+    if ((nk > 0 && !knot_vector) || (nc > 0 && !ctrl_pts)) return fail(GCV_ERR_INVALID, "NULL knots or control points");
+    if (w == GCV_HOST) {
+        const std::vector<double> kv = widen_host(knot_vector, (size_t)nk), cp = widen_host(ctrl_pts, (size_t)nc);
+        return gcv_create_bsplines(out, n_curve, degree, dim, knots_offset, kv.data(), cp.data(), GCV_HOST, opt);
+    }
+    // device data: widened into buffers the context then owns
+    DBuf<double> kv, cp;
+    gcv_status r = kv.reserve((size_t)nk);
+    if (r == GCV_OK) r = cp.reserve((size_t)nc);
+    if (r == GCV_OK) {
+        cudaStream_t st = opt ? (cudaStream_t)opt->stream : nullptr;
+        if (nk) k_widen<<<convert_grid(nk), 256, 0, st>>>(knot_vector, kv.p, nk);
+        if (nc) k_widen<<<convert_grid(nc), 256, 0, st>>>(ctrl_pts, cp.p, nc);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) r = cuda_fail(e, "widening the FP32 curve data");
+    }
+    gcv_ctx* c = nullptr;
+    if (r == GCV_OK) r = gcv_create_bsplines(&c, n_curve, degree, dim, knots_offset, kv.p, cp.p, GCV_DEVICE, opt);
+    if (r != GCV_OK) {
+        kv.release();
+        cp.release();
+        return r;
+    }
+    // hand the widened arrays to the context (it borrowed them)
+    c->knots.owned = true;
+    c->knots.bytes = kv.bytes;
+    c->ctrl.owned = true;
+    c->ctrl.bytes = cp.bytes;
+    kv.p = nullptr;
+    cp.p = nullptr;
+    *out = c;
+    return GCV_OK;
+}
+
+gcv_status gcv_get_all_curve_arclengths_f32(gcv_ctx* ctx, float* out, int where)
+{
+    if (!ctx || !out) return fail(GCV_ERR_INVALID, "NULL argument");
+    if (!ctx->table_ready) return fail(GCV_ERR_STATE, "createArclengthTable has not run");
+    const int64_t n = ctx->n_curve;
+    if (n == 0) return GCV_OK;
+    float* d = out;
+    if (where != GCV_DEVICE) {
+        CHECK(ctx->f32_buf.reserve((size_t)n));
+        d = ctx->f32_buf.p;
+    }
+    k_narrow<<<convert_grid(n), 256, 0, ctx->stream>>>(ctx->curve_len.p, d, n);
+    CU(cudaGetLastError());
+    if (where != GCV_DEVICE) {
+        CU(cudaMemcpyAsync(out, d, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+    }
+    return GCV_OK;
+}
+
+gcv_status gcv_get_arclength_f32(gcv_ctx* ctx, int cid, float* out)
+{
+    if (!out) return fail(GCV_ERR_INVALID, "NULL argument");
+    double v = 0.0;
+    CHECK(gcv_get_arclength(ctx, cid, &v));
+    *out = (float)v;
+    return GCV_OK;
+}
+
+gcv_status gcv_arclength_reverse_into_f32(gcv_ctx* ctx, const int* n_ptrs_for_curves, const float* sample_position,
+                                          int is_relative, int in_where, int what, float* out, int out_where)
+{
+    if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
+    if (!ctx->table_ready) return fail(GCV_ERR_STATE, "createArclengthTable has not run");
+    if (what != GCV_RETURN_US && what != GCV_RETURN_POINTS) return fail(GCV_ERR_INVALID, "what must be RETURN_US or RETURN_POINTS");
+    if (in_where != GCV_HOST && in_where != GCV_DEVICE) return fail(GCV_ERR_INVALID, "bad in_where");
+    if (out_where != GCV_HOST && out_where != GCV_DEVICE) return fail(GCV_ERR_INVALID, "bad out_where");
+    if (ctx->n_curve > 0 && !n_ptrs_for_curves) return fail(GCV_ERR_INVALID, "n_ptrs_for_curves is NULL");
+    int64_t total = 0;
+    CHECK(stage_counts(ctx, n_ptrs_for_curves, in_where, &total));
+    if (total == 0) return GCV_OK;
+    if (!sample_position || !out) return fail(GCV_ERR_INVALID, "NULL positions or output");
+    const int width = what == GCV_RETURN_US ? 1 : ctx->point_dim;
+    const int64_t n_out = total * width;
+    CHECK(ctx->sample_pos.reserve((size_t)total));
+    CHECK(ctx->sample_out.reserve((size_t)n_out));
+    const int64_t n_f = std::max<int64_t>(in_where == GCV_HOST ? total : 0, out_where == GCV_HOST ? n_out : 0);
+    if (n_f) CHECK(ctx->f32_buf.reserve((size_t)n_f));
+    const float* d_in = sample_position;
+    if (in_where == GCV_HOST) {
+        CU(cudaMemcpyAsync(ctx->f32_buf.p, sample_position, (size_t)total * sizeof(float), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        d_in = ctx->f32_buf.p;
+    }
+    k_widen<<<convert_grid(total), 256, 0, ctx->stream>>>(d_in, ctx->sample_pos.p, total);
+    CU(cudaGetLastError());
+    CHECK(run_sampling(ctx, ctx->sample_off.p, ctx->sample_pos.p, total, is_relative ? 1 : 0, what, ctx->sample_out.p,
+                       nullptr, nullptr));
+    float* d_out = out_where == GCV_DEVICE ? out : ctx->f32_buf.p;
+    k_narrow<<<convert_grid(n_out), 256, 0, ctx->stream>>>(ctx->sample_out.p, d_out, n_out);
+    CU(cudaGetLastError());
+    if (out_where == GCV_HOST) {
+        CU(cudaMemcpyAsync(out, d_out, (size_t)n_out * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+    }
+    return GCV_OK;
+}
+
+gcv_status gcv_arclength_reverse_f32(gcv_ctx* ctx, const int* n_ptrs_for_curves, const float* sample_position,
+                                     int is_relative, int where, int what, gcv_result_f32* result)
+{
+    if (!ctx || !result) return fail(GCV_ERR_INVALID, "NULL argument");
+    std::memset(result, 0, sizeof(*result));
+    if (!ctx->table_ready) return fail(GCV_ERR_STATE, "createArclengthTable has not run");
+    if (where != GCV_HOST && where != GCV_DEVICE) return fail(GCV_ERR_INVALID, "where must be GCV_HOST or GCV_DEVICE");
+    if (what != GCV_RETURN_US && what != GCV_RETURN_POINTS) return fail(GCV_ERR_INVALID, "what must be RETURN_US or RETURN_POINTS");
+    if (ctx->n_curve > 0 && !n_ptrs_for_curves) return fail(GCV_ERR_INVALID, "n_ptrs_for_curves is NULL");
+    int64_t total = 0;
+    for (int64_t i = 0; i < ctx->n_curve; ++i) {
+        if (n_ptrs_for_curves[i] < 0) return fail(GCV_ERR_INVALID, "negative sample count");
+        total += n_ptrs_for_curves[i];
+    }
+    const int width = what == GCV_RETURN_US ? 1 : ctx->point_dim;
+    result->n_points = total;
+    result->store_where = where;
+    result->store_what = what;
+    result->point_dim = width;
+    const size_t bytes = (size_t)std::max<int64_t>(total, 1) * width * sizeof(float);
+    if (where == GCV_DEVICE) {
+        CU(cudaMalloc(&result->data, bytes));
+    } else {
+        result->data = (float*)std::malloc(bytes);
+        if (!result->data) return fail(GCV_ERR_OUT_OF_MEMORY, "host result allocation failed");
+    }
+    gcv_status st = gcv_arclength_reverse_into_f32(ctx, n_ptrs_for_curves, sample_position, is_relative, GCV_HOST,
+                                                   what, result->data, where);
+    if (st != GCV_OK) {
+        gcv_free_result_f32(result);
+        return st;
+    }
+    if (where == GCV_DEVICE) CU(cudaStreamSynchronize(ctx->stream));
+    return GCV_OK;
+}
+
+gcv_status gcv_free_result_f32(gcv_result_f32* r)
 {
     if (!r) return fail(GCV_ERR_INVALID, "result is NULL");
     if (r->data) {

@@ -246,6 +246,35 @@ gcv_status gcv_measure_fma_peak(int which, double* tflops);
  * buffers of every device; *bytes (may be NULL) receives how many bytes. */
 gcv_status gcv_release_cached_memory(int64_t* bytes);
 
+/* ---- FP32 data ------------------------------------------------------------
+ * The reference's float instantiation, ArclengthCalculateGpu<float> (the
+ * samples' default, samples/sample1_ellipse/main.cpp:16-20,
+ * samples/sample2_bspline/main.cpp:19): the same calls with float curve
+ * data, positions, lengths, parameters and points.  Inputs are widened to
+ * double and the work runs as for double data (options.precision and rtol as
+ * given; GCV_MIXED with rtol 1e-6 matches the reference's float tolerance
+ * MAX_ERROR_FLOAT, gcurval/config.h:31); results are rounded to float.
+ * Device FP32 B-spline data is widened into buffers the context owns. */
+typedef struct gcv_result_f32 {
+    int64_t n_points;
+    int store_where;
+    int store_what;
+    int point_dim;
+    float* data;
+} gcv_result_f32;
+
+gcv_status gcv_create_ellipses_f32(gcv_ctx** out, int n_curve, const float* a, const float* b, const float* rot,
+                                   const float* cx, const float* cy, int where, const gcv_options* opt);
+gcv_status gcv_create_bsplines_f32(gcv_ctx** out, int n_curve, int degree, int dim, const int* knots_offset,
+                                   const float* knot_vector, const float* ctrl_pts, int where, const gcv_options* opt);
+gcv_status gcv_get_all_curve_arclengths_f32(gcv_ctx* ctx, float* out, int where);
+gcv_status gcv_get_arclength_f32(gcv_ctx* ctx, int cid, float* out);
+gcv_status gcv_arclength_reverse_into_f32(gcv_ctx* ctx, const int* n_ptrs_for_curves, const float* sample_position,
+                                          int is_relative, int in_where, int what, float* out, int out_where);
+gcv_status gcv_arclength_reverse_f32(gcv_ctx* ctx, const int* n_ptrs_for_curves, const float* sample_position,
+                                     int is_relative, int where, int what, gcv_result_f32* result);
+gcv_status gcv_free_result_f32(gcv_result_f32* result);
+
 /* ---- allocation-free lengths ---------------------------------------------- */
 
 /* Largest number of knot intervals gcv_bspline_lengths_noalloc accepts. */
