@@ -40,6 +40,20 @@ constexpr int MLP_NPARAM = MLP_OFF_B4 + MLP_OUT;
 constexpr float GELU_C = 0.7978845608028654f;
 constexpr float GELU_A = 0.044715f;
 
+// x to float by its bit pattern, truncated (integer instructions only: on
+// GB300 a conversion on the FP64 pipe costs as much issue time as dozens of
+// FP32 instructions); |x| below 2^-126 gives 0, above 2^127 the largest float.
+// Precise enough for the network's features.
+__device__ __forceinline__ float float_of(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned top = (unsigned)(b >> 32), sign = top & 0x80000000u;
+    const int e = (int)((top >> 20) & 0x7FFu) - 1023;
+    if (e < -126) return __uint_as_float(sign);
+    if (e > 127) return __uint_as_float(sign | 0x7F7FFFFFu);
+    return __uint_as_float(sign | ((unsigned)(e + 127) << 23) | (unsigned)((b >> 29) & 0x7FFFFFull));
+}
+
 // Features of interval s (a B-spline knot interval; anything else gets
 // zeros), FP32:
 //   0 degree / 5, 1 dim - 2,
@@ -51,7 +65,7 @@ constexpr float GELU_A = 0.044715f;
 //        to [-8, 8], / 8,
 //   14 log2(polygon length / chord) clamped to [0, 8], / 4,
 //   15 -log10(rtol) / 10.
-// Computed in FP32 apart from the knot and control-point differences.
+// Computed in FP32 from the knots and control points converted by float_of.
 __device__ inline void interval_features(const Batch& b, int64_t s, float log_rtol_feature, float* f)
 {
 #pragma unroll
@@ -63,18 +77,18 @@ __device__ inline void interval_features(const Batch& b, int64_t s, float log_rt
     const double* kv = b.knots + b.knot_off[c];
     const double* cp = b.ctrl + b.ctrl_off[c];
     const int span = int(j) + p;
-    // knot differences in FP64 (near-duplicate knots), the rest in FP32
     const double k0 = kv[span];
-    const float w = (float)(kv[span + 1] - k0);
+    const float fk0 = float_of(k0);
+    const float w = float_of(kv[span + 1]) - fk0;
     f[0] = p * 0.2f;
     f[1] = (float)(D - 2);
     f[15] = log_rtol_feature;
     if (!(w > 0.0f)) return;
     // control polygon of the interval, relative to its first point
-    float q[6][3];
+    float q[6][3], base[3];
+    for (int d = 0; d < 3; ++d) base[d] = d < D ? float_of(cp[(size_t)(span - p) * D + d]) : 0.0f;
     for (int i = 0; i <= p; ++i)
-        for (int d = 0; d < 3; ++d)
-            q[i][d] = d < D ? (float)(cp[(size_t)(span - p + i) * D + d] - cp[(size_t)(span - p) * D + d]) : 0.0f;
+        for (int d = 0; d < 3; ++d) q[i][d] = d < D ? float_of(cp[(size_t)(span - p + i) * D + d]) - base[d] : 0.0f;
     float e[5], sum = 0.0f;
     for (int i = 0; i < p; ++i) {
         const float dx = q[i + 1][0] - q[i][0], dy = q[i + 1][1] - q[i][1], dz = q[i + 1][2] - q[i][2];
@@ -95,9 +109,9 @@ __device__ inline void interval_features(const Batch& b, int64_t s, float log_rt
         const float chord = sqrtf(cx * cx + cy * cy + cz * cz);
         f[14] = chord > 0.0f ? fminf(fmaxf(__log2f(sum / chord), 0.0f), 8.0f) * 0.25f : 2.0f;
     }
-    const float support = (float)(kv[span + p + 1] - kv[span - p]);
+    const float support = float_of(kv[span + p + 1]) - float_of(kv[span - p]);
     f[11] = support > 0.0f ? w / support : 0.0f;
-    const float wl = (float)(k0 - kv[span - 1]), wr = (float)(kv[span + 2] - kv[span + 1]);
+    const float wl = fk0 - float_of(kv[span - 1]), wr = float_of(kv[span + 2]) - float_of(kv[span + 1]);
     f[12] = wl > 0.0f ? fminf(fmaxf(__log2f(wl / w), -8.0f), 8.0f) * 0.125f : -1.0f;
     f[13] = wr > 0.0f ? fminf(fmaxf(__log2f(wr / w), -8.0f), 8.0f) * 0.125f : -1.0f;
 }

@@ -4,7 +4,8 @@
 // intervals (M = 128 rows, one row per thread and TMEM lane):
 //   features (FP32 rows, written by k_feature_rows) -> bf16 tile X [128 x 16]
 //   D = X W1        1 x tcgen05.mma (K = 16), D in TMEM (128 lanes x 128 cols, FP32)
-//   H1 = GELU(D + b1) -> bf16 tile [128 x 128] in shared memory
+//   H1 = 2 GELU(D + b1) -> bf16 tile [128 x 128] in shared memory (the
+//        factor 2 is taken back by W2, W3, W4 stored halved: exact in bf16)
 //   D = H1 W2, H2, D = H2 W3, H3: 8 MMAs each (K = 128 in steps of 16)
 //   D = H3 W4 (N = 32): outputs -> start depths of the length walk (or raw)
 // The transposed weights W^T (N x K) stay in shared memory for the whole
@@ -34,8 +35,9 @@ constexpr int WB_W4 = 0;                                // W4^T [32][128]
 constexpr int WB_W1 = WB_W4 + MLP_OUT * MLP_H * 2;      // W1^T [128][16]
 constexpr int WB_W2 = WB_W1 + MLP_H * MLP_IN * 2;       // W2^T [128][128]
 constexpr int WB_W3 = WB_W2 + MLP_H * MLP_H * 2;        // W3^T [128][128]
-constexpr int WB_BIAS = WB_W3 + MLP_H * MLP_H * 2;      // b1, b2, b3 (128 each), b4 (32), FP32
-constexpr int WB_BYTES = WB_BIAS + (3 * MLP_H + MLP_OUT) * 4;
+constexpr int WB_B4 = WB_W3 + MLP_H * MLP_H * 2;        // b4 (32), FP32
+constexpr int WB_BH = WB_B4 + MLP_OUT * 4;              // b1, b2, b3 (128 each), bf16 pairs
+constexpr int WB_BYTES = WB_BH + 3 * MLP_H * 2;
 constexpr int NWG = 4;                                  // warpgroups per CTA
 constexpr int SM_X = (WB_BYTES + 127) / 128 * 128;      // NWG X tiles [128][16] bf16
 constexpr int X_BYTES = 128 * MLP_IN * 2;
@@ -139,22 +141,23 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r)
         : "memory");
 }
 
-// GELU of two values in packed bf16x2 arithmetic (the activations are stored
-// as bf16 for the next layer anyway): 0.5 x (1 + tanh(c x (1 + a x^2)))
-__device__ __forceinline__ uint32_t gelu_bf16x2(float x0, float x1)
+// Twice the GELU of two accumulator values plus their bias, in packed bf16x2
+// arithmetic (the activations are stored as bf16 for the next layer
+// anyway): with x = acc + b, 2 GELU(x) = x (1 + tanh(x (c + c a x^2))),
+// c = sqrt(2/pi), a = 0.044715.  Six instructions per pair.
+__device__ __forceinline__ uint32_t gelu2_bf16x2(float x0, float x1, uint32_t b)
 {
     uint32_t x, r;
     asm("cvt.rn.bf16x2.f32 %0, %2, %1;" : "=r"(x) : "f"(x0), "f"(x1));
-    asm("{\n\t.reg .b32 x2, y, u, t, hx;\n\t"
-        "mul.rn.bf16x2 x2, %1, %1;\n\t"
-        "fma.rn.bf16x2 y, x2, %2, %3;\n\t"    // 1 + a x^2
-        "mul.rn.bf16x2 u, %1, y;\n\t"
-        "mul.rn.bf16x2 u, u, %4;\n\t"         // c x (1 + a x^2)
+    asm("{\n\t.reg .b32 xb, x2, y, u, t;\n\t"
+        "add.rn.bf16x2 xb, %1, %2;\n\t"      // + bias
+        "mul.rn.bf16x2 x2, xb, xb;\n\t"
+        "fma.rn.bf16x2 y, x2, %3, %4;\n\t"   // c a x^2 + c
+        "mul.rn.bf16x2 u, xb, y;\n\t"
         "tanh.approx.bf16x2 t, u;\n\t"
-        "mul.rn.bf16x2 hx, %1, %5;\n\t"       // x / 2
-        "fma.rn.bf16x2 %0, t, hx, hx;\n\t}\n"
+        "fma.rn.bf16x2 %0, t, xb, xb;\n\t}\n"
         : "=r"(r)
-        : "r"(x), "r"(0x3D373D37u), "r"(0x3F803F80u), "r"(0x3F4C3F4Cu), "r"(0x3F003F00u));
+        : "r"(x), "r"(b), "r"(0x3D123D12u), "r"(0x3F4C3F4Cu));
     return r;
 }
 
@@ -189,7 +192,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
     const int tid = threadIdx.x, wg = tid >> 7, t = tid & 127, warp = tid >> 5;
     uint64_t* bars = reinterpret_cast<uint64_t*>(sm + SM_BAR);
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(sm + SM_BAR + 8 * NWG);
-    const float* bias = reinterpret_cast<const float*>(sm + WB_BIAS);
+    const float* bias4 = reinterpret_cast<const float*>(sm + WB_B4);
+    const uint32_t* bias_h = reinterpret_cast<const uint32_t*>(sm + WB_BH);
 
     // weights into shared memory
     for (int i = tid; i < WB_BYTES / 16; i += TC_THREADS)
@@ -270,7 +274,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
             if (!ok) break;
             if (layer < 3) {
                 // epilogue: bias + GELU -> bf16 H (the MMAs reading H have completed)
-                const float* bl = bias + layer * MLP_H;
+                const uint32_t* bl = bias_h + layer * (MLP_H / 2);
                 // 64 columns per TMEM load (two loads per layer)
 #pragma unroll 1
                 for (int c2 = 0; c2 < MLP_H / 64; ++c2) {
@@ -282,8 +286,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
                         uint32_t h[16];
 #pragma unroll
                         for (int i = 0; i < 16; ++i)
-                            h[i] = gelu_bf16x2(__uint_as_float(v[32 * half + 2 * i]) + bl[32 * c + 2 * i],
-                                               __uint_as_float(v[32 * half + 2 * i + 1]) + bl[32 * c + 2 * i + 1]);
+                            h[i] = gelu2_bf16x2(__uint_as_float(v[32 * half + 2 * i]),
+                                                __uint_as_float(v[32 * half + 2 * i + 1]), bl[16 * c + i]);
 #pragma unroll
                         for (int q = 0; q < 4; ++q)
                             *reinterpret_cast<uint4*>(H + kmaj_off(t, 32 * c + 8 * q, MLP_H)) =
@@ -298,9 +302,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
                 uint32_t r[32];
                 tmem_ld32(tlane, r);
                 float o[32];
-                const float* bl = bias + 3 * MLP_H;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) o[i] = __uint_as_float(r[i]) + bl[i];
+                for (int i = 0; i < 32; ++i) o[i] = __uint_as_float(r[i]) + bias4[i];
                 if (live) {
                     if constexpr (STARTS) {
                         const int64_t s = A.list ? (int64_t)A.list[A.row0 + row] : A.row0 + row;
@@ -365,22 +368,27 @@ cudaError_t launch_tc(const TcArgs& A, cudaStream_t stream)
 std::vector<uint8_t> weight_image(const float* w)
 {
     std::vector<uint8_t> img(WB_BYTES, 0);
-    auto put = [&](int base, int N, int K, int off) {  // W[k][n] (K x N) -> W^T core-matrix tile
+    // W[k][n] (K x N) -> W^T core-matrix tile, times `scale` (1 or 1/2: exact)
+    auto put = [&](int base, int N, int K, int off, float scale) {
         for (int n = 0; n < N; ++n)
             for (int k = 0; k < K; ++k) {
-                const __nv_bfloat16 h = __float2bfloat16_rn(w[off + k * N + n]);
+                const __nv_bfloat16 h = __float2bfloat16_rn(w[off + k * N + n] * scale);
                 std::memcpy(&img[(size_t)base + kmaj_off(n, k, K)], &h, 2);
             }
     };
-    put(WB_W1, MLP_H, MLP_IN, MLP_OFF_W1);
-    put(WB_W2, MLP_H, MLP_H, MLP_OFF_W2);
-    put(WB_W3, MLP_H, MLP_H, MLP_OFF_W3);
-    put(WB_W4, MLP_OUT, MLP_H, MLP_OFF_W4);
-    float* b = reinterpret_cast<float*>(&img[WB_BIAS]);
-    std::memcpy(b, w + MLP_OFF_B1, MLP_H * 4);
-    std::memcpy(b + MLP_H, w + MLP_OFF_B2, MLP_H * 4);
-    std::memcpy(b + 2 * MLP_H, w + MLP_OFF_B3, MLP_H * 4);
-    std::memcpy(b + 3 * MLP_H, w + MLP_OFF_B4, MLP_OUT * 4);
+    // the hidden activations are stored as 2 GELU: the layers reading them
+    // take the 1/2
+    put(WB_W1, MLP_H, MLP_IN, MLP_OFF_W1, 1.0f);
+    put(WB_W2, MLP_H, MLP_H, MLP_OFF_W2, 0.5f);
+    put(WB_W3, MLP_H, MLP_H, MLP_OFF_W3, 0.5f);
+    put(WB_W4, MLP_OUT, MLP_H, MLP_OFF_W4, 0.5f);
+    std::memcpy(&img[WB_B4], w + MLP_OFF_B4, MLP_OUT * 4);
+    const int boff[3] = {MLP_OFF_B1, MLP_OFF_B2, MLP_OFF_B3};
+    for (int l = 0; l < 3; ++l)
+        for (int i = 0; i < MLP_H; ++i) {
+            const __nv_bfloat16 h = __float2bfloat16_rn(w[boff[l] + i]);
+            std::memcpy(&img[(size_t)WB_BH + (size_t)(l * MLP_H + i) * 2], &h, 2);
+        }
     return img;
 }
 
