@@ -140,6 +140,32 @@ struct EvalFF {
             return ff_sqrt(s);
         }
     }
+    // speed and q in plain FP32 from the coefficients' leading parts: for the
+    // leaf table's f and q, which only shape the sampler's initial guess
+    __device__ __forceinline__ static float speed_slope32(const ff* r, float v, float& q)
+    {
+        if constexpr (CODE == 0) {
+            float sn, cs;
+            sincospif(fmaf(v, (float)ELLIPSE_PIECE_SCALE, r[2].hi), &sn, &cs);
+            q = (float)(PI * ELLIPSE_PIECE_SCALE) * r[0].hi * sn * cs;
+            return sqrtf(fmaf(r[0].hi, sn * sn, r[1].hi));
+        } else {
+            float s = 0.0f, t = 0.0f;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                float acc = r[(P - 1) * D + d].hi, dacc = 0.0f;
+#pragma unroll
+                for (int k = P - 2; k >= 0; --k) {
+                    dacc = fmaf(dacc, v, acc);
+                    acc = fmaf(acc, v, r[k * D + d].hi);
+                }
+                s = fmaf(acc, acc, s);
+                t = fmaf(acc, dacc, t);
+            }
+            q = t;
+            return sqrtf(s);
+        }
+    }
 };
 
 // ------------------------------------------- symbolic de Boor set-up (FF)
@@ -236,8 +262,7 @@ constexpr bool panel_rolled()
 }
 
 template <int CODE>
-__device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, int depth, ff& K, ff& G, ff& fend,
-                                             float& qend)
+__device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, int depth, ff& K, ff& G)
 {
     const float hw = __int_as_float((127 - depth) << 23);  // 2^-depth, exact
     const float kh = (float)(unsigned)(k >> 24), kl = (float)(unsigned)(k & 0xFFFFFFull);
@@ -264,7 +289,6 @@ __device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, 
             if (i & 1) gg = ff_fma(to_ff(split_const(gk_wg(i))), s, gg);
         }
     }
-    fend = EvalFF<CODE>::speed_slope(r, ff_add_f(vlo, 2.0f * hw), qend);
     K = ff_scale(kk, hw);
     G = ff_scale(gg, hw);
 }
@@ -280,15 +304,30 @@ __device__ __forceinline__ void load_ff_dyn(int code, const float2* __restrict__
     }
 }
 
-__device__ __forceinline__ void panel_ff_dyn(int code, const ff* r, unsigned long long k, int depth, ff& K, ff& G,
-                                             ff& fend, float& qend)
+__device__ __forceinline__ void panel_ff_dyn(int code, const ff* r, unsigned long long k, int depth, ff& K, ff& G)
 {
     switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: panel_k15_ff<C>(r, k, depth, K, G, fend, qend); break;
+    case C: panel_k15_ff<C>(r, k, depth, K, G); break;
         GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
-    default: K = G = fend = ff{0.0f, 0.0f}; qend = 0.0f; break;
+    default: K = G = ff{0.0f, 0.0f}; break;
+    }
+}
+
+template <int CODE>
+__device__ __forceinline__ float speed_slope32_of(int code, const ff* r, float v, float& q)
+{
+    if constexpr (CODE >= 0) {
+        return EvalFF<CODE>::speed_slope32(r, v, q);
+    } else {
+        switch (code) {
+#define GCV_CASE(C)                                                                                \
+    case C: return EvalFF<C>::speed_slope32(r, v, q);
+            GCV_FOR_EACH_CODE(GCV_CASE)
+#undef GCV_CASE
+        default: q = 0.0f; return 0.0f;
+        }
     }
 }
 

@@ -200,19 +200,19 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
         // ---- one panel per active lane
         if (active) {
             // panel values: K15, the error test, and (for leaves) the right-end
-            // speed f and slope q in FP64; the float-float path keeps its
-            // values in FP32 pairs and touches FP64 only for leaves and for
-            // error tests that land within 1 % of the threshold
+            // speed f and slope q, in FP64; the float-float path keeps its
+            // values in FP32 pairs, evaluates f and q of leaves in plain FP32,
+            // and touches FP64 only for leaves' sums and for error tests that
+            // land within 1 % of the threshold
             bool ok, finite;
             double K = 0.0, fend = 0.0, qend = 0.0;
-            ff Kf{0.0f, 0.0f}, fendf{0.0f, 0.0f};
-            float q32 = 0.0f;
+            ff Kf{0.0f, 0.0f};
             if constexpr (PREC == 1) {
                 ff Gf;
                 if constexpr (CODE >= 0)
-                    panel_k15_ff<(CODE >= 0 ? CODE : 0)>(rf, k, depth, Kf, Gf, fendf, q32);
+                    panel_k15_ff<(CODE >= 0 ? CODE : 0)>(rf, k, depth, Kf, Gf);
                 else
-                    panel_ff_dyn(code, rf, k, depth, Kf, Gf, fendf, q32);
+                    panel_ff_dyn(code, rf, k, depth, Kf, Gf);
                 if (depth == 0) {
                     tol_unit = P.rtol * fabs(ff_to_double(Kf));
                     tol_f = (float)tol_unit;
@@ -250,7 +250,11 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                 if constexpr (PREC == 1) {
                     cumf = ff_add(cumf, Kf);
                     cum = ff_to_double(cumf);
-                    fend = ff_to_double(fendf);
+                    // the leaf's right-end speed and slope (FP32: they only
+                    // shape the sampler's guess), -1 + (k + 1) 2^(1 - depth)
+                    const float vr32 = fmaf((float)(k + 1), __int_as_float((128 - depth) << 23), -1.0f);
+                    float q32;
+                    fend = (double)speed_slope32_of<CODE>(code, rf, vr32, q32);
                     qend = (double)q32;
                 } else {
                     cum += K;
