@@ -66,15 +66,18 @@ gcv_status cuda_fail(cudaError_t e, const char* what)
 // contexts of one batch shape then maps and unmaps none of the ~100 GB a
 // 1M-curve table holds.  Buffers enter the cache only after a device-wide
 // synchronisation (what cudaFree would have done), so a cached block is idle.
-// A cudaMalloc that runs out of memory frees the cache and tries again.
+// A cudaMalloc that runs out of memory frees the oldest cached blocks (those
+// least likely to be asked for again) until it succeeds.
 // GCV_NO_MEMORY_CACHE=1 in the environment turns the cache off;
 // gcv_release_cached_memory() frees it.
 struct CachedBlock {
     void* p;
     int dev;
+    unsigned long long seq;  // order of entry
 };
 std::mutex g_cache_m;
 std::multimap<size_t, CachedBlock> g_cache;  // by size in bytes
+unsigned long long g_cache_seq = 0;
 
 bool cache_enabled()
 {
@@ -118,6 +121,29 @@ size_t release_cache(int dev)
     return bytes;
 }
 
+// frees the oldest cached blocks of device `dev` until `want` bytes are
+// freed (or none is left); returns the bytes freed
+size_t release_oldest(int dev, size_t want)
+{
+    std::vector<void*> drop;
+    size_t bytes = 0;
+    {
+        std::lock_guard<std::mutex> g(g_cache_m);
+        while (bytes < want) {
+            auto oldest = g_cache.end();
+            for (auto it = g_cache.begin(); it != g_cache.end(); ++it)
+                if (it->second.dev == dev && (oldest == g_cache.end() || it->second.seq < oldest->second.seq))
+                    oldest = it;
+            if (oldest == g_cache.end()) break;
+            drop.push_back(oldest->second.p);
+            bytes += oldest->first;
+            g_cache.erase(oldest);
+        }
+    }
+    for (void* q : drop) cudaFree(q);
+    return bytes;
+}
+
 // a block of at least `bytes`; *got = its size
 cudaError_t dev_alloc(void** p, size_t bytes, size_t* got)
 {
@@ -134,9 +160,10 @@ cudaError_t dev_alloc(void** p, size_t bytes, size_t* got)
         }
     }
     cudaError_t e = cudaMalloc(p, bytes);
-    if (e == cudaErrorMemoryAllocation && cache_enabled()) {
+    while (e == cudaErrorMemoryAllocation && cache_enabled()) {
         cudaGetLastError();
-        if (release_cache(dev) > 0) e = cudaMalloc(p, bytes);
+        if (release_oldest(dev, bytes) == 0) break;
+        e = cudaMalloc(p, bytes);
     }
     *got = e == cudaSuccess ? bytes : 0;
     return e;
@@ -151,7 +178,7 @@ void dev_recycle(void* p, size_t bytes)
         return;
     }
     std::lock_guard<std::mutex> g(g_cache_m);
-    g_cache.insert({bytes, CachedBlock{p, current_device()}});
+    g_cache.insert({bytes, CachedBlock{p, current_device(), ++g_cache_seq}});
 }
 
 template <typename T>
