@@ -124,6 +124,38 @@ __device__ __forceinline__ int sample_curve(const SampleParams& P, int64_t i, in
     return upper_bound_i64(P.sample_off, int(P.b.n_curve) + 1, i);
 }
 
+// The curve of sample i with a per-thread memory of the last curve found:
+// a thread that meets the same curve again skips the binary search (the
+// mixed sampler hands each warp runs of consecutive samples).
+struct CurveHint {
+    int64_t lo = 0, hi = 0;  // sample range (list order) of the remembered curve
+    int64_t shift = 0;       // its global sample index minus the list-order one
+    int c = 0;
+};
+__device__ __forceinline__ int sample_curve_hint(const SampleParams& P, int64_t i, int64_t& gi, CurveHint& h)
+{
+    if (i >= h.lo && i < h.hi) {
+        gi = i + h.shift;
+        return h.c;
+    }
+    if (P.curve_list) {
+        const int64_t j = P.cb + upper_bound_i64(P.list_off + P.cb, int(P.ce - P.cb) + 1, i);
+        h.c = P.curve_list[j];
+        h.lo = P.list_off[j];
+        h.hi = P.list_off[j + 1];
+        h.shift = P.sample_off[h.c] - h.lo;
+    } else {
+        h.c = upper_bound_i64(P.sample_off, int(P.b.n_curve) + 1, i);
+        h.lo = P.sample_off[h.c];
+        h.hi = P.sample_off[h.c + 1];
+        h.shift = 0;
+    }
+    gi = i + h.shift;
+    return h.c;
+}
+// samples per warp and turn in the mixed sampler (8 per lane, 32 apart)
+constexpr int SAMPLE_RUN = 256;
+
 constexpr int SAMPLE_THREADS = 256;      // default block size
 constexpr int SAMPLE_THREADS_MAX = 512;  // largest block size the autotuner tries
 constexpr int NEWTON_MAXIT = 16;

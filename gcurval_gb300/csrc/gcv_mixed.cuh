@@ -104,10 +104,16 @@ __global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample_ff(SampleParams P
     unsigned long long newton = 0;
     int64_t i0, i1;
     sample_range(P, i0, i1);
-    for (int64_t ii = i0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; ii < i1;
-         ii += (int64_t)gridDim.x * blockDim.x) {
+    // each warp takes runs of SAMPLE_RUN consecutive samples, 32 at a time:
+    // a lane's samples then mostly share their curve (see CurveHint)
+    CurveHint hint;
+    const int lane = threadIdx.x & 31;
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t run = i0 + wid * SAMPLE_RUN; run < i1; run += n_warps * SAMPLE_RUN)
+    for (int64_t ii = run + lane; ii < run + SAMPLE_RUN && ii < i1; ii += 32) {
         int64_t i;
-        const int c = sample_curve(P, ii, i);
+        const int c = sample_curve_hint(P, ii, i, hint);
         const int code = CODE >= 0 ? CODE : curve_code(b, c);
         const int64_t s0 = b.seg_off[c], s1 = b.seg_off[c + 1];
         int64_t s;
