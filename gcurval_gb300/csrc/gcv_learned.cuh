@@ -5,7 +5,7 @@
 // fractions (j + 1/2) / 8 of the interval.  The length walk starts at the
 // predicted depths instead of the whole interval; every panel is still
 // checked with the Kronrod error estimate and split further when it misses
-// the tolerance, so the plain adaptive method remains the judge.
+// the tolerance, so the plain adaptive method keeps the final say.
 //
 // This header: sizes, the packed weight layout, the per-interval features and
 // the start-depth rule shared by the kernels.
