@@ -76,3 +76,31 @@ def test_null_handles_rejected():
     assert lib.gcv_destroy(None) == _lib.GCV_ERR_INVALID
     assert lib.gcv_create_arclength_table(None) == _lib.GCV_ERR_INVALID
     assert lib.gcv_free_result(None) == _lib.GCV_ERR_INVALID
+
+
+def test_bundle_and_f32_arguments_rejected_without_gpu():
+    lib = g.load()
+    h = ctypes.c_void_p()
+    text = b"3 4 8\n0 1 2 3\n0 1 0 1\n0 0 0 0 1 1 1 1\n"
+    off = (ctypes.c_int64 * 2)(0, len(text))
+    bad_off = (ctypes.c_int64 * 2)(0, len(text) - 1)
+    assert lib.gcv_bundle_parse(text, len(text), off, 0, -1, 2, _lib.GCV_HOST, None, ctypes.byref(h)) == \
+        _lib.GCV_ERR_INVALID
+    assert lib.gcv_bundle_parse(text, len(text), bad_off, 1, -1, 2, _lib.GCV_HOST, None, ctypes.byref(h)) == \
+        _lib.GCV_ERR_INVALID
+    assert b"n_bytes" in lib.gcv_last_error()
+    assert lib.gcv_bundle_parse(text, len(text), off, 1, -1, 4, _lib.GCV_HOST, None, ctypes.byref(h)) == \
+        _lib.GCV_ERR_INVALID
+    assert lib.gcv_bundle_parse(text, len(text), off, 1, -1, 2, 7, None, ctypes.byref(h)) == _lib.GCV_ERR_INVALID
+    assert lib.gcv_bundle_sizes(None, None, None, None) == _lib.GCV_ERR_INVALID
+    o = g.default_options()
+    kv = np.zeros(8, np.float32)
+    cp = np.zeros(8, np.float32)
+    ko = np.array([0, 8], np.int32)
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert lib.gcv_create_bsplines_f32(ctypes.byref(h), 1, 7, 2, ptr(ko), ptr(kv), ptr(cp), _lib.GCV_HOST,
+                                       ctypes.byref(o)) == _lib.GCV_ERR_INVALID
+    assert lib.gcv_create_bsplines_f32(ctypes.byref(h), 1, 3, 4, ptr(ko), ptr(kv), ptr(cp), _lib.GCV_HOST,
+                                       ctypes.byref(o)) == _lib.GCV_ERR_INVALID
+    assert lib.gcv_create_ellipses_f32(ctypes.byref(h), -1, None, None, None, None, None, _lib.GCV_HOST,
+                                       ctypes.byref(o)) == _lib.GCV_ERR_INVALID
