@@ -96,8 +96,16 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
 // quintic-Hermite guess in FP32, Newton on the leaf in float-float
 // (G8 partial integral on the shorter side, local to the leaf), and the
 // final update of v in FP64.
+// Registers per thread are capped (blocks of up to SAMPLE_THREADS_MAX threads
+// still fit): left to itself the compiler gave the degree-4/5 codes 95-117
+// registers, and the occupancy lost cost more than a cap costs.  80 leaves
+// every code spill-free but degree-5 3D, which gets 88 (spill-free there).
+// Sampling of the uneven 1M batch: 215.7 ms uncapped, 203.6 with 80 for
+// every code, 202.6 with 88 for degree-5 3D.
+__host__ __device__ constexpr int sample_ff_regs(int code) { return code == bs_code(5, 3) ? 88 : 80; }
+static_assert(88 * SAMPLE_THREADS_MAX <= 65536, "a block of SAMPLE_THREADS_MAX must fit one SM");
 template <int CODE>
-__global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample_ff(SampleParams P, const float2* __restrict__ coef_ff)
+__global__ void __maxnreg__(sample_ff_regs(CODE)) k_sample_ff(SampleParams P, const float2* __restrict__ coef_ff)
 {
     const Batch& b = P.b;
     const Table& t = P.t;
