@@ -1,0 +1,29 @@
+"""bench.py --impl reference on the CPU: the reference's CPU implementation of
+the path (the compiled driver where the reference tree exists, else the
+oracle's port) prints one JSON line with the bench contract's keys, on the
+same metric and unit as the GPU arm, with a zero-copy e2e block."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_the_contract_line():
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--n-curves", "2000", "--steps", "1",
+                        "--warmup", "1"], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["impl"] == "reference"
+    assert d["unit"] == "curves/s" and d["higher_is_better"] is True
+    assert d["metric"].startswith("curves/s")
+    assert d["value"] > 0 and d["ms_per_step"] > 0
+    assert d["steps"] == 1 and d["warmup"] >= 3
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]
+    assert cb["value"] == d["value"]
+    e2e = d["e2e"]
+    assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
+    assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    assert d["config"]["workload"].startswith("uneven_batch")
