@@ -112,7 +112,8 @@ _SIGS = {
                                                  ctypes.POINTER(ResultF32)]),
     "gcv_free_result_f32": (ctypes.c_int, [ctypes.POINTER(ResultF32)]),
     "gcv_bspline_lengths_noalloc": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
-                                                   ctypes.c_double, ctypes.c_int, _P, _P]),
+                                                   ctypes.c_double, ctypes.c_int, _P, _P,
+                                                   ctypes.POINTER(ctypes.c_int64)]),
     # learned form (include/gcurval_gb300_learned.h)
     "gcv_mlp_param_count": (ctypes.c_int, []),
     "gcv_mlp_last_error": (ctypes.c_char_p, []),

@@ -290,18 +290,24 @@ gcv_status gcv_free_result_f32(gcv_result_f32* result);
  * knots_offset[n_curve + 1], knot_vector, ctrl_pts, and the output
  * lengths[n_curve].  The result equals gcv_create_arclength_table +
  * gcv_get_all_curve_arclengths (FP64, same rtol / max_depth) to rounding.
+ * knots_offset is checked on the device before anything reads through it:
+ * it must start at 0 and give every curve at least 2 degree + 1 knots, else
+ * GCV_ERR_INVALID with the allocating path's message.  n_capped (host
+ * pointer, may be NULL) receives the number of panels accepted at max_depth
+ * without meeting rtol, as gcv_stats.n_capped does for the allocating path.
  * The call allocates nothing: its working memory is one static device array
  * of GCV_NOALLOC_MAX_INTERVALS doubles plus a 256-byte header (about 8 MiB),
  * held by every GPU that loads the library until the process exits; batches
  * with more knot intervals return GCV_ERR_INVALID.  The first call on a device
- * looks up that array's address with the device current; make it before any
- * stream capture.  All calls share the array, so calls whose GPU work
- * overlaps race and must be serialised by the caller.  Runs on `stream`
- * (cudaStream_t, NULL = legacy default stream) and waits for it before
- * returning. */
+ * looks up that array's address with the device current and keeps it for the
+ * life of the process: make that first call before any stream capture begins,
+ * and make no call on a device after cudaDeviceReset.  Runs on `stream`
+ * (cudaStream_t, NULL = legacy default stream) and waits for that stream
+ * before returning.  All calls share the array, so calls whose GPU work
+ * overlaps race and must be serialised by the caller. */
 gcv_status gcv_bspline_lengths_noalloc(int n_curve, int degree, int dim, const int* knots_offset,
                                        const double* knot_vector, const double* ctrl_pts, double rtol,
-                                       int max_depth, double* lengths, void* stream);
+                                       int max_depth, double* lengths, void* stream, int64_t* n_capped);
 
 #ifdef __cplusplus
 }

@@ -40,6 +40,7 @@
 
 #include <math.h>
 #include <pthread.h>
+#include <stdatomic.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -272,7 +273,8 @@ static void build_curve(gcvo_table* t, int c, uint64_t* evals)
 typedef struct job {
     void (*fn)(struct job*, int);
     gcvo_table* t;
-    int lo, hi;
+    atomic_int* next; /* shared: the next curve to take */
+    int n;
     const int* n_per_curve;
     const int64_t* off;
     const double* pos;
@@ -282,10 +284,18 @@ typedef struct job {
     uint64_t evals;
 } job_t;
 
+/* Curves are taken one at a time from a shared counter (dynamic
+ * scheduling): per-curve costs are heavy-tailed (a 4,096-point curve costs
+ * thousands of times a 4-point one), so static ranges leave most threads
+ * idle behind the one that drew the largest curves. */
 static void* job_main(void* arg)
 {
     job_t* j = (job_t*)arg;
-    for (int c = j->lo; c < j->hi; c++) j->fn(j, c);
+    for (;;) {
+        const int c = atomic_fetch_add_explicit(j->next, 1, memory_order_relaxed);
+        if (c >= j->n) break;
+        j->fn(j, c);
+    }
     return NULL;
 }
 
@@ -295,10 +305,12 @@ static void run_jobs(job_t* proto, int n, int nthreads)
     if (nthreads > n) nthreads = n > 0 ? n : 1;
     job_t* jobs = (job_t*)calloc((size_t)nthreads, sizeof(job_t));
     pthread_t* th = (pthread_t*)calloc((size_t)nthreads, sizeof(pthread_t));
+    atomic_int next;
+    atomic_init(&next, 0);
     for (int i = 0; i < nthreads; i++) {
         jobs[i] = *proto;
-        jobs[i].lo = (int)((int64_t)n * i / nthreads);
-        jobs[i].hi = (int)((int64_t)n * (i + 1) / nthreads);
+        jobs[i].next = &next;
+        jobs[i].n = n;
         jobs[i].evals = 0;
         if (nthreads > 1)
             pthread_create(&th[i], NULL, job_main, &jobs[i]);
@@ -585,6 +597,18 @@ void gcvo_point(const gcvo_batch* b, int cid, double u, double* out)
     while (seg + 1 < nseg && u >= kv[seg + p + 1]) seg++;
     pack_t pk = make_pack(b, cid, seg, &ev);
     point(&pk, u, out);
+}
+
+/* C(u) evaluated on knot interval segid of curve cid (span segid + degree),
+ * as a plugin's GetPoint does with the pack of that interval
+ * (samples/sample2_bspline/structs.h:165-174); -1 for a bad segid. */
+int gcvo_point_seg(const gcvo_batch* b, int cid, int segid, double u, double* out)
+{
+    uint64_t ev = 0;
+    if (segid < 0 || segid >= curve_segments(b, cid)) return -1;
+    pack_t pk = make_pack(b, cid, segid, &ev);
+    point(&pk, u, out);
+    return 0;
 }
 
 /* the two-pi constant is part of the ellipse knot convention */

@@ -65,6 +65,7 @@ void gcvo_s_at_many(const gcvo_table* t, const int* n_per_curve, const double* u
 /* |C'(u)| of curve cid at parameter u, and C(u) (dim doubles). */
 double gcvo_speed(const gcvo_batch* b, int cid, double u);
 void gcvo_point(const gcvo_batch* b, int cid, double u, double* out);
+int gcvo_point_seg(const gcvo_batch* b, int cid, int segid, double u, double* out);
 
 /* Work counters: total table entries, and total |C'| evaluations. */
 int64_t gcvo_table_entries(const gcvo_table* t);

@@ -19,7 +19,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libgcv_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libgcv_ref.so")
-REF_TREE = os.environ.get("GCV_REFERENCE_TREE", "/root/reference")
+# The reference source tree, read only to compile its CPU driver; it exists
+# on the development host only.  GCV_REFERENCE_TREE overrides the location.
+REF_TREE = os.environ.get("GCV_REFERENCE_TREE") or "/root/reference"
 
 # the reference's defaults for double: MAX_ERROR_DOUBLE (gcurval/config.h:32)
 # and MaxRecursiveDepth<double> (gcurval/config.h:42)
@@ -66,6 +68,7 @@ def _load_port():
         lib.gcvo_speed.restype = ctypes.c_double
         lib.gcvo_speed.argtypes = [ctypes.POINTER(_Batch), ctypes.c_int, ctypes.c_double]
         lib.gcvo_point.argtypes = [ctypes.POINTER(_Batch), ctypes.c_int, ctypes.c_double, _P]
+        lib.gcvo_point_seg.argtypes = [ctypes.POINTER(_Batch), ctypes.c_int, ctypes.c_int, ctypes.c_double, _P]
         lib.gcvo_table_entries.restype = ctypes.c_int64
         lib.gcvo_table_entries.argtypes = [_P]
         lib.gcvo_evals.restype = ctypes.c_int64
@@ -153,6 +156,16 @@ class Oracle:
         self.lib.gcvo_point(ctypes.byref(self._b), cid, u, _ptr(out))
         return out
 
+    def point_on_segment(self, cid: int, segid: int, u: float) -> np.ndarray:
+        """C(u) from the polynomial piece of knot interval segid (u may be
+        either end of it)."""
+        if not 0 <= cid < self.batch.n_curve:
+            raise IndexError(cid)
+        out = np.zeros(3)
+        if self.lib.gcvo_point_seg(ctypes.byref(self._b), cid, segid, u, _ptr(out)) != 0:
+            raise IndexError(segid)
+        return out
+
     def table_entries(self) -> int:
         return int(self.lib.gcvo_table_entries(self.h))
 
@@ -196,6 +209,10 @@ def _load_ref():
         lib.gcvref_bspline_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P, _P,
                                            ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int]
         lib.gcvref_max_error.restype = ctypes.c_double
+        lib.gcvref_load_bundle.argtypes = [ctypes.c_char_p, ctypes.c_int, _P, _P, ctypes.c_int, _P, ctypes.c_int]
+        lib.gcvref_ellipse_rule.argtypes = [ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int, _P, _P, _P]
+        lib.gcvref_bspline_rule.argtypes = [ctypes.c_int, ctypes.c_int, _P, _P, ctypes.c_int, ctypes.c_int, _P, _P,
+                                            _P]
         _ref = lib
     return _ref
 
@@ -250,3 +267,45 @@ class Reference:
         if out is not None and what:
             out = out.reshape(-1, 2 if self.is_ellipse else self.d)
         return lengths, out
+
+
+def reference_load_bundle(path: str, n_curve: int):
+    """(knots_offset int32[n+1], knots, ctrl (n_points, 2)) of the first
+    n_curve curves of a Bundle file, read and normalised by the reference's
+    own loader (samples/sample2_bspline/dataset_loader.h:40-126)."""
+    lib = _load_ref()
+    cap = 64 * n_curve + 64
+    ko = np.zeros(n_curve + 1, np.int32)
+    kv = np.zeros(cap)
+    cp = np.zeros(2 * cap)
+    nk = lib.gcvref_load_bundle(path.encode(), n_curve, _ptr(ko), _ptr(kv), cap, _ptr(cp), cap)
+    if nk < 0:
+        raise RuntimeError("the reference loader's output does not fit (or n_curve is outside 1..1000)")
+    n_pts = nk - 4 * n_curve
+    return ko, kv[:nk].copy(), cp[:2 * n_pts].reshape(-1, 2).copy()
+
+
+RULE_IDS = {"polyline": 0, "simpson": 1, "vincent_forsey": 2}
+
+
+def reference_rule_values(rule: str, begin, end, ellipse=None, bspline=None) -> np.ndarray:
+    """The reference's own point-based rule functors (gcurval/base/functors.inl.h:
+    145-238) on [begin[i], end[i]]: of the ellipse (a, b) (x = a cos t,
+    y = b sin t), or of one cubic 2D B-spline (knots, ctrl (n, 2), segid) on
+    its knot interval segid."""
+    lib = _load_ref()
+    b = np.ascontiguousarray(begin, np.float64)
+    e = np.ascontiguousarray(end, np.float64)
+    out = np.zeros(b.size)
+    if ellipse is not None:
+        rc = lib.gcvref_ellipse_rule(RULE_IDS[rule], float(ellipse[0]), float(ellipse[1]), b.size, _ptr(b), _ptr(e),
+                                     _ptr(out))
+    else:
+        kv, cp, segid = bspline
+        kv = np.ascontiguousarray(kv, np.float64)
+        cp = np.ascontiguousarray(cp, np.float64)
+        rc = lib.gcvref_bspline_rule(RULE_IDS[rule], cp.shape[0], _ptr(kv), _ptr(cp), int(segid), b.size, _ptr(b),
+                                     _ptr(e), _ptr(out))
+    if rc != 0:
+        raise ValueError("bad rule or knot interval")
+    return out

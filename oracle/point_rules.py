@@ -17,26 +17,39 @@ limit; the result is L + R.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 POLYLINE, SIMPSON, VINCENT_FORSEY = "polyline", "simpson", "vincent_forsey"
 
 
+def _norm(v) -> float:
+    """sqrt(x0^2 + x1^2 (+ x2^2)), summed left to right like a fixed-size
+    vector's norm()."""
+    s = 0.0
+    for x in v:
+        s += float(x) * float(x)
+    return math.sqrt(s)
+
+
 def rule(kind: str, a, m, b) -> float:
+    """The rule from the points a = C(begin), m = C(mid), b = C(end), with the
+    reference's operations in its order (so equal points give equal bits)."""
     a, m, b = (np.asarray(x, np.float64) for x in (a, m, b))
-    nrm = np.linalg.norm
     if kind == POLYLINE:
-        return float(nrm(b - a))
+        return _norm(b - a)
     if kind == SIMPSON:
-        return float((nrm(-3.0 * a + 4.0 * m - b) + 4.0 * nrm(b - a) + nrm(a - 4.0 * m + 3.0 * b)) / 6.0)
+        return 1.0 / 6.0 * (_norm(-3.0 * a + 4.0 * m - b) + 4.0 * _norm(b - a) + _norm(a - 4.0 * m + 3.0 * b))
     if kind == VINCENT_FORSEY:
-        return float(4.0 / 3.0 * (nrm(a - m) + nrm(b - m)) - 1.0 / 3.0 * nrm(b - a))
+        return 4.0 / 3.0 * (_norm(a - m) + _norm(b - m)) - 1.0 / 3.0 * _norm(b - a)
     raise ValueError(kind)
 
 
 def rule_on(kind: str, point, t0: float, t1: float) -> float:
-    """The rule on [t0, t1] of the curve point(t)."""
-    return rule(kind, point(t0), point(0.5 * (t0 + t1)), point(t1))
+    """The rule on [t0, t1] of the curve point(t); the midpoint is
+    (t0 + t1) / 2 as in the reference."""
+    return rule(kind, point(t0), point((t0 + t1) / 2.0), point(t1))
 
 
 def adaptive_length(kind: str, point, t0: float, t1: float, eps0: float, max_depth: int = 23) -> float:

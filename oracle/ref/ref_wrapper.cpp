@@ -20,7 +20,9 @@
 
 #include <gcurval/gcurval.h>
 #include <samples/sample2_bspline/BSpline.h>
+#include <samples/sample2_bspline/dataset_loader.h>
 
+#include <atomic>
 #include <chrono>
 #include <cstring>
 #include <thread>
@@ -247,7 +249,11 @@ double now_s()
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-// Shard [0, n) into nthreads contiguous ranges and run fn(lo, hi) on each.
+// Run fn(lo, hi) over [0, n) on nthreads threads, in chunks taken from a
+// shared counter (dynamic scheduling: per-curve costs are heavy-tailed, so
+// static ranges leave most threads idle behind the largest curves).  Each
+// chunk builds its own calculator, as a harness sharding curves over
+// std::threads with one calculator per shard does.
 template <typename F>
 void run_sharded(int n, int nthreads, F fn)
 {
@@ -257,12 +263,19 @@ void run_sharded(int n, int nthreads, F fn)
         return;
     }
     if (nthreads > n) nthreads = n;
+    const int chunk = std::max(1, n / (nthreads * 16));
+    std::atomic<int> next(0);
     std::vector<std::thread> th;
     for (int t = 0; t < nthreads; ++t)
     {
-        int lo = int((long long)n * t / nthreads);
-        int hi = int((long long)n * (t + 1) / nthreads);
-        th.emplace_back([=]() { fn(lo, hi); });
+        th.emplace_back([&]() {
+            for (;;)
+            {
+                const int lo = next.fetch_add(chunk);
+                if (lo >= n) break;
+                fn(lo, std::min(n, lo + chunk));
+            }
+        });
     }
     for (auto& x : th) x.join();
 }
@@ -330,6 +343,22 @@ int bspline_run(int n, const int* knots_offset, const double* knots, const doubl
     return 0;
 }
 
+// The reference's point-based length rules (gcurval/base/functors.inl.h:
+// PolylineMethod :145-165, SimpsonMethod :167-206, VincentForseyRule
+// :208-238) on [begin[i], end[i]] of one curve, through the curve plugins'
+// GetPoint: rule 0 polyline, 1 Simpson, 2 Vincent-Forsey.
+template <typename Rule, typename GetPoint, typename Pack>
+void rule_values(int n, const double* begin, const double* end, const Pack& pk, double* out)
+{
+    for (int i = 0; i < n; ++i) out[i] = Rule()(begin[i], end[i], GetPoint(), pk);
+}
+
+template <typename Rule, typename GetPoint, typename Pack, typename Scratch>
+void rule_values(int n, const double* begin, const double* end, const Pack& pk, Scratch& sc, double* out)
+{
+    for (int i = 0; i < n; ++i) out[i] = Rule()(begin[i], end[i], GetPoint(), pk, sc);
+}
+
 } // namespace
 
 extern "C" {
@@ -374,6 +403,72 @@ long long gcvref_ellipse_table_entries(int n, const double* a, const double* b)
     EllipseCalc<double> c(n, a, b);
     c.createArclengthTable();
     return c.entries();
+}
+
+// The reference's dataset loader (load_dataset / read_a_curve,
+// samples/sample2_bspline/dataset_loader.h:40-126) on one Bundle file: the
+// first n_curve (<= 1000) curves as 2D points, centred and scaled as that
+// loader does.  Copies knots_offset[n_curve + 1], the knots and the control
+// points (x, y pairs) out; returns the number of knots, or -1 when they do
+// not fit the caller's capacities (knots_cap doubles, ctrl_cap points).
+// The loader itself holds 50 knots and 50 points per curve on average.
+int gcvref_load_bundle(const char* path, int n_curve, int* knots_offset, double* knots, int knots_cap,
+                       double* ctrl, int ctrl_cap)
+{
+    using Pt = gcurval::Vector2X<double>;
+    if (n_curve < 1 || n_curve > 1000) return -1;
+    const char* names[1] = {path};
+    CurveSet<double, Pt>* cs = load_dataset<double, Pt>(n_curve, names, 1);
+    const int nk = cs->knots_offset[n_curve];
+    const int np = nk - (cs->degree + 1) * n_curve;
+    int rc = nk;
+    if (nk > knots_cap || np > ctrl_cap)
+    {
+        rc = -1;
+    }
+    else
+    {
+        std::memcpy(knots_offset, cs->knots_offset, sizeof(int) * (n_curve + 1));
+        std::memcpy(knots, cs->knot_vector, sizeof(double) * nk);
+        for (int i = 0; i < np; ++i)
+        {
+            ctrl[2 * i] = cs->ctrl_ptrs[i][0];
+            ctrl[2 * i + 1] = cs->ctrl_ptrs[i][1];
+        }
+    }
+    delete cs;
+    return rc;
+}
+
+int gcvref_ellipse_rule(int rule, double a, double b, int n, const double* begin, const double* end, double* out)
+{
+    RefEllipsePack<double> pk(0.0, 2 * EIGEN_PI, 0, 0, a, b);
+    using GP = RefEllipsePoint<double>;
+    if (rule == 0) rule_values<gcurval::PolylineMethod<double>, GP>(n, begin, end, pk, out);
+    else if (rule == 1) rule_values<gcurval::SimpsonMethod<double>, GP>(n, begin, end, pk, out);
+    else if (rule == 2) rule_values<gcurval::VincentForseyRule<double>, GP>(n, begin, end, pk, out);
+    else return -1;
+    return 0;
+}
+
+// one cubic 2D B-spline (n_ctrl points, n_ctrl + 4 knots) on knot interval
+// segid (span segid + 3), parameters inside that interval
+int gcvref_bspline_rule(int rule, int n_ctrl, const double* knots, const double* ctrl, int segid, int n,
+                        const double* begin, const double* end, double* out)
+{
+    using Pt = gcurval::Vector2X<double>;
+    constexpr int P = 3;
+    if (segid < 0 || segid >= n_ctrl - P) return -1;
+    RefBSplinePack<double, Pt> pk(0.0, 0.0, 0, segid, segid + P, const_cast<double*>(knots),
+                                  reinterpret_cast<Pt*>(const_cast<double*>(ctrl)));
+    std::vector<uint8_t> buf(RefScratchAllocator<double, P>::size());
+    const RefScratch<double> sc = RefScratchAllocator<double, P>()(buf.data());
+    using GP = RefBSplinePoint<double, Pt, P>;
+    if (rule == 0) rule_values<gcurval::PolylineMethod<double>, GP>(n, begin, end, pk, sc, out);
+    else if (rule == 1) rule_values<gcurval::SimpsonMethod<double>, GP>(n, begin, end, pk, sc, out);
+    else if (rule == 2) rule_values<gcurval::VincentForseyRule<double>, GP>(n, begin, end, pk, sc, out);
+    else return -1;
+    return 0;
 }
 
 double gcvref_max_error(void) { return double(gcurval::MAX_ERROR_DOUBLE); }

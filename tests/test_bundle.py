@@ -62,3 +62,21 @@ def test_device_number_conversion_matches_strtod(tmp_path):
     r = subprocess.run([exe, "200000"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout[-2000:]
     assert "mismatched 0" in r.stdout
+
+
+def test_host_reader_equals_the_reference_loader_on_real_curves(tmp_path):
+    """tests/golden/bundle_0.npz holds the text of the first 300 records of
+    the reference's dataset/BSpline/Bundle_0.txt and the arrays the
+    reference's own load_dataset made of them (compiled from the reference
+    by make_golden.py): the host reader gives the same bits."""
+    import os
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "bundle_0.npz"))
+    assert str(z["loader"]) == "reference load_dataset"
+    f = tmp_path / "bundle_0_head.txt"
+    f.write_bytes(z["text"].tobytes())
+    b = bundle.load(str(f), samples_per_curve=9)
+    assert b.n_curve == 300
+    np.testing.assert_array_equal(b.knot_off, z["knot_off"])
+    np.testing.assert_array_equal(b.ctrl_off, z["ctrl_off"])
+    assert np.array_equal(b.knots.view(np.uint64), z["knots"].view(np.uint64))
+    assert np.array_equal(b.ctrl.view(np.uint64), z["ctrl"].view(np.uint64))

@@ -75,6 +75,16 @@ def test_real_curves_unnormalised_give_the_fixture_arrays(gpu_lib):
     assert np.max(np.abs(L - z["ref_lengths"]) / z["ref_lengths"]) <= 1e-9
 
 
+def test_real_curves_give_the_reference_loaders_arrays(gpu_lib):
+    """The device reader on the text of the reference's first 300 dataset
+    records (kept in the fixture) gives, bit for bit, what the reference's
+    own load_dataset made of them (the fixture's arrays)."""
+    b, z = load_golden("bundle_0")
+    assert str(z["loader"]) == "reference load_dataset"
+    dev = bundle.load_device(z["text"].tobytes(), normalize=True)
+    assert_same(dev, (b.kind, b.degree, b.dim, b.knot_off, b.knots, b.ctrl_off, b.ctrl))
+
+
 @pytest.mark.parametrize("dim", [2, 3])
 def test_real_curves_normalised_like_the_host_reader(gpu_lib, dim):
     _, _, degrees, ctrls, knots = golden_curves()
