@@ -2,18 +2,31 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload uniform_bsplines|ellipses|mixed3d_bsplines|uneven_batch]
-                    [--precision plain|mixed]
+                    [--precision plain|mixed|learned]
 
 A step is one pass of the hot path over one batch: createArclengthTable plus
 arclengthReverse of every sample of every curve.  Prints ONE JSON line (rank 0).
 
-* ``value``  curves/s with the batch already resident in HBM (device-timed with
-             CUDA events around each step; L2 is flushed between steps).
-* ``e2e``    the same metric through the public API with host buffers: context
-             creation from host arrays (H2D), table, sampling into host memory
-             (H2D positions, D2H parameters), destroy; wall clock per step.
-* ``roofline`` for the dominant kernel, ``cpu_baseline`` (the reference's CPU
-             algorithm on a bounded sample, all host threads), ``clocks``.
+* ``value``    curves/s with the batch already resident in HBM (device-timed with
+               CUDA events around each step on the step's own stream; L2 is
+               flushed on that stream before each step, outside the events).
+* ``e2e``      the same metric through the public API with host buffers: context
+               creation from host arrays (H2D), table, sampling into host memory
+               (H2D positions, D2H parameters), destroy; wall clock per step.
+* ``roofline`` for the dominant phase: algorithmic FLOPs (evaluations of the
+               plain FP64 method x FLOPs per evaluation as the reference's de
+               Boor / ellipse derivative costs them) over the phase's time,
+               against the FMA peak of the pipe the form runs on; the library's
+               own per-evaluation count beside it.
+* ``cpu_baseline`` the reference's CPU algorithm on cost-stratified samples of
+               the workload: one thread and all host threads, at the reference's
+               default tolerance and at one matched to the accuracy target.
+* ``accuracy_vs_fp64_oracle`` every form on a stratified sample of the batch
+               plus its hardest curves (most near-duplicate knots, degree 5,
+               most intervals, most samples), against the FP64 oracle.
+* ``configs``  the other measured workloads (4,096 ellipses and 10,000 uniform
+               cubics in plain FP64, 100,000 3D degree-3/5 curves in mixed
+               precision), each with its value, roofline, accuracy and CPU baseline.
 
 N > 1 (torchrun): every rank runs its own batch of the full size (weak
 scaling, independent curves, no collective on the data path); the step time
@@ -25,6 +38,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -53,6 +67,25 @@ WORKLOADS = {
                      "tolerance 5e-9 for the 1e-8 accuracy target"),
 }
 
+# The other workloads, measured beside the headline in the form each is quoted in.
+CONFIG_RUNS = (("C1", "ellipses", "plain"), ("C2", "uniform_bsplines", "plain"), ("C3", "mixed3d_bsplines", "mixed"))
+
+# Accuracy bar of each precision form (relative length and sample-position error).
+ACCURACY_BAR = {"plain": 1e-10, "mixed": 1e-8, "learned": 1e-8}
+
+# The reference's CPU algorithm at its default FP64 tolerance (MAX_ERROR_DOUBLE,
+# gcurval/config.h:32) and at an absolute tolerance matched to the 1e-8 target.
+REF_MAX_ERROR = 1e-14
+MATCHED_MAX_ERROR = 1e-8
+# Curves in the CPU baseline's cost-stratified samples: (all host threads, one
+# thread) per tolerance, sized for a few seconds each.
+CPU_SAMPLES = {
+    "uneven_batch": {"default": (512, 48), "matched": (4096, 512)},
+    "ellipses": {"default": (4096, 512), "matched": (4096, 512)},
+    "uniform_bsplines": {"default": (2048, 256), "matched": (4096, 512)},
+    "mixed3d_bsplines": {"default": (1024, 96), "matched": (2048, 192)},
+}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -66,10 +99,14 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=3,
                     help="timed steps of the plain FP64 form on the same batch, for the speed-up (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--config-steps", type=int, default=10, help="timed steps of each per-config run")
+    ap.add_argument("--no-configs", action="store_true", help="skip the per-config runs")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the accuracy checks against the oracle")
     ap.add_argument("--no-graph", action="store_true",
                     help="device-resident steps through the ordinary calls instead of the captured CUDA graph")
-    ap.add_argument("--cpu-sample-curves", type=int, default=0, help="curves in the CPU-baseline sample (0: auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-curves", type=int, default=0,
+                    help="curves of the CPU sample at the default tolerance, all threads (0: the workload's default)")
     ap.add_argument("--n-curves", type=int, default=0, help="override the workload's curve count (profiling runs)")
     return ap.parse_args()
 
@@ -143,83 +180,159 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------- CPU side
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else platform)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith("model name"):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.processor() or platform.machine()
+
+
 def cpu_sample(batch, n_curves: int):
-    idx = np.linspace(0, batch.n_curve - 1, n_curves).astype(np.int64)
-    sub = batch.subset(np.unique(idx))
+    """A cost-stratified sample of n_curves curves (largest first), with positions."""
+    from gcurval_gb300 import datasets as ds
+    sub = batch.subset(ds.stratified_indices(batch, n_curves))
     sub.sample_positions()
     return sub
 
 
-def _groups(batch):
-    """Curve subsets of one (kind, degree, dim): the reference's CPU driver
-    is instantiated per curve type, as its sample programs are."""
-    key = batch.kind.astype(np.int64) * 100 + batch.degree.astype(np.int64) * 10 + batch.dim.astype(np.int64)
-    return [batch.subset(np.nonzero(key == k)[0]) for k in np.unique(key)]
-
-
-def run_cpu_reference(sub, nthreads: int, prefer_reference: bool = True):
+def run_cpu_reference(sub, nthreads: int, max_error: float = REF_MAX_ERROR):
     """One pass of the reference CPU algorithm over `sub` (table + sampling of
-    every sample): (seconds, kind).  Batches that mix curve types run one
-    reference calculator per type, back to back."""
+    every sample): (seconds, kind).  The reference's own driver, compiled
+    from its tree where that exists, runs at its built-in tolerance: one
+    calculator per curve (the driver is instantiated per curve type), taken
+    largest first by a pool of nthreads threads.  Other tolerances, and hosts
+    without the tree, run the oracle's restatement of it (bit-identical to
+    the compiled driver at the same tolerance), whose C thread pool takes
+    curves one at a time from a shared counter."""
     from oracle import oracle as orc
-    if prefer_reference and orc.reference_available():
-        parts = _groups(sub)
-        for p in parts:
+    if max_error == REF_MAX_ERROR and orc.reference_available():
+        from concurrent.futures import ThreadPoolExecutor
+        from gcurval_gb300 import datasets as ds
+        order = np.argsort(-ds.cost_proxy(sub), kind="stable")
+        items = []
+        for i in order:
+            p = sub.subset([i])
             p.sample_positions()
-        refs = [orc.Reference(p, nthreads=nthreads) for p in parts]
+            items.append((p, orc.Reference(p, nthreads=1)))
+        run = lambda it: it[1].run(it[0].n_samples, it[0].positions, True, 0)
         t0 = time.perf_counter()
-        for p, ref in zip(parts, refs):
-            ref.run(p.n_samples, p.positions, True, 0)
+        if nthreads <= 1:
+            for it in items:
+                run(it)
+        else:
+            with ThreadPoolExecutor(max_workers=nthreads) as ex:
+                list(ex.map(run, items))  # ctypes releases the GIL during each call
         return time.perf_counter() - t0, "reference"
     t0 = time.perf_counter()
-    o = orc.Oracle(sub, nthreads=nthreads)
+    o = orc.Oracle(sub, max_error=max_error, nthreads=nthreads)
     o.reverse(sub.n_samples, sub.positions, True, 0)
     return time.perf_counter() - t0, "port"
 
 
-def accuracy_vs_oracle(sub, precision, rtol, model=None):
+def cpu_baseline(batch, workload: str, nthreads: int, n_default: int = 0) -> dict:
+    """The reference's CPU algorithm on cost-stratified samples of the batch:
+    all host threads and one thread, at the default and at the matched
+    tolerance.  ``value`` is all threads at the default tolerance.
+    n_default overrides that run's sample size (and scales the others)."""
+    sizes = CPU_SAMPLES[workload]
+    scale = n_default / sizes["default"][0] if n_default else 1.0
+    runs = []
+    for tol_name, max_error in (("default", REF_MAX_ERROR), ("matched", MATCHED_MAX_ERROR)):
+        n_all, n_one = (max(1, int(round(x * scale))) for x in sizes[tol_name])
+        for threads, n in ((nthreads, n_all), (1, n_one)):
+            sub = cpu_sample(batch, n)
+            secs, kind = run_cpu_reference(sub, threads, max_error)
+            nseg = int(sub.n_segments.sum())
+            runs.append({"threads": threads, "tolerance": tol_name, "max_error": max_error, "kind": kind,
+                         "curves": int(sub.n_curve), "samples": int(sub.total_samples), "intervals": nseg,
+                         "seconds": round(secs, 3), "curves_per_s": round(sub.n_curve / secs, 3),
+                         "samples_per_s": round(sub.total_samples / secs, 1),
+                         "intervals_per_s": round(nseg / secs, 1)})
+    head = runs[0]
+    return {"value": head["curves_per_s"], "unit": "curves/s", "cores": nthreads, "kind": head["kind"],
+            "sample": (f"{head['curves']} curves, a cost-stratified sample of the workload ({head['samples']} "
+                       f"samples, {head['intervals']} knot intervals), table + sampling, all {nthreads} host "
+                       f"threads, absolute tolerance {REF_MAX_ERROR:g} (the reference's default)"),
+            "samples_per_s": head["samples_per_s"], "intervals_per_s": head["intervals_per_s"],
+            "cpu_model": cpu_model(), "nproc": os.cpu_count(), "runs": runs}
+
+
+def accuracy_vs_oracle(sub, forms: dict, rtol: float, model=None) -> dict:
     """Relative total-length error and sample-position error |s(u) - target| / L
-    of the library on `sub` against the FP64 oracle (the reference's CPU
-    algorithm restated), maxima over the subset."""
+    of the library's forms on `sub` against the FP64 oracle (the reference's
+    CPU algorithm restated, its tolerance scaled to each curve's size),
+    maxima over the subset.  forms: name -> (precision, learned)."""
     import gcurval_gb300 as g
     from oracle import oracle as orc
-    calc = g.ArclengthCalculateGpu.from_batch(sub, precision=precision, rtol=rtol, learned=model is not None)
-    if model is not None:
-        calc.set_learned_model(model)
-    try:
-        calc.createArclengthTable()
-        L = calc.getAllCurveArclengths()
-        u = calc.arclengthReverse(sub.n_samples, sub.positions, True, g.GCV_HOST).us
-    finally:
-        calc.close()
-    o = orc.Oracle(sub)
+    t0 = time.perf_counter()
+    o = orc.ScaledOracle(sub)
     Lo = o.lengths()
-    s = o.s_at(sub.n_samples, u)
     tgt = sub.positions * np.repeat(Lo, sub.n_samples)
     Lrep = np.maximum(np.repeat(Lo, sub.n_samples), 1e-300)
+    out = {}
+    for name, (prec, learned) in forms.items():
+        calc = g.ArclengthCalculateGpu.from_batch(sub, precision=prec, rtol=rtol, learned=learned)
+        if learned:
+            calc.set_learned_model(model)
+        try:
+            calc.createArclengthTable()
+            L = calc.getAllCurveArclengths()
+            u = calc.arclengthReverse(sub.n_samples, sub.positions, True, g.GCV_HOST).us
+        finally:
+            calc.close()
+        s = o.s_at(sub.n_samples, u)
+        le = np.abs(L - Lo) / np.maximum(Lo, 1e-300)
+        se = np.abs(s - tgt) / Lrep if s.size else np.zeros(1)
+        out[name] = {"max_rel_length_err": float(np.max(le)), "max_rel_sample_err": float(np.max(se)),
+                     "worst_curve_samples": int(np.argmax(se)) if s.size else -1,
+                     "bar": ACCURACY_BAR.get(name, 1e-8)}
     return {"curves": int(sub.n_curve), "samples": int(sub.total_samples),
-            "max_rel_length_err": float(np.max(np.abs(L - Lo) / np.maximum(Lo, 1e-300))),
-            "max_rel_sample_err": float(np.max(np.abs(s - tgt) / Lrep)) if s.size else 0.0,
-            "oracle": "oracle/ C restatement of ArclengthCalculateCpu, FP64"}
+            "intervals": int(sub.n_segments.sum()), "forms": out, "seconds": round(time.perf_counter() - t0, 2),
+            "oracle": "oracle/ C restatement of ArclengthCalculateCpu, FP64, MAX_ERROR 1e-16 x control-polygon length"}
 
 
-def auto_cpu_curves(batch, nthreads: int, target_s: float) -> int:
-    """Curves of the CPU sample: a pilot of 32 curves spread over the batch,
-    timed, scaled to about `target_s` seconds on `nthreads` threads."""
-    pilot = cpu_sample(batch, min(32, batch.n_curve))
-    secs, _ = run_cpu_reference(pilot, nthreads)
-    n = int(pilot.n_curve * target_s / max(secs, 1e-3))
-    return int(max(16, min(batch.n_curve, n)))
+def accuracy_subset(batch, n_stratified: int, k_hard: int):
+    from gcurval_gb300 import datasets as ds
+    sub = batch.subset(ds.accuracy_subset_indices(batch, n_stratified, k_hard))
+    sub.sample_positions()
+    return sub
 
 
-# --------------------------------------------------------------- our arm
+# --------------------------------------------------------- FLOP counting
 def flops_per_eval(batch) -> float:
-    """FP64 flops of one |C'| evaluation (add/mul/sqrt/div 1, FMA 2), batch mean."""
+    """This library's FP64-equivalent FLOPs of one |C'| evaluation (add, mul,
+    sqrt 1, FMA 2) on its per-interval polynomials, batch mean over curves."""
     p = batch.degree.astype(np.float64)
     d = batch.dim.astype(np.float64)
     bs = d * 2.0 * np.maximum(p - 1, 0) + (2.0 * d - 1.0) + 1.0  # Horner, squared norm, sqrt
     ell = 1.0 + 2.0 + 2.0 + 1.0 + 20.0  # s^2, fma, sqrt, scale + sinpi (counted as 20)
     return float(np.mean(np.where(batch.kind == 0, ell, bs)))
+
+
+def survey_flops_per_eval(batch, weight) -> float:
+    """FLOPs of one |C'(t)| evaluation as the reference computes it (de Boor
+    basis and derivative, samples/sample2_bspline/BSpline.h:50-96 with
+    gcurval/base/functors.inl.h:51-63; ellipse 12): B-spline of degree p in
+    dimension D: 2(p-1) + 2.5 p(p-1) + 2 + 4p + D(2p+1) + 2D + 4 (51 for a
+    2D cubic, 101 for a 3D quintic).  Mean over curves weighted by `weight`
+    (intervals for the length phase, samples for sampling)."""
+    p = batch.degree.astype(np.float64)
+    d = batch.dim.astype(np.float64)
+    bs = 2 * (p - 1) + 2.5 * p * (p - 1) + 2 + 4 * p + d * (2 * p + 1) + 2 * d + 4
+    f = np.where(batch.kind == 0, 12.0, bs)
+    w = np.asarray(weight, np.float64)
+    return float(np.sum(f * w) / max(np.sum(w), 1.0))
 
 
 # ------------------------------------------------------- multi-rank glue
@@ -237,6 +350,198 @@ def job_throughput(units_per_rank: int, ms_per_step_max: float, world: int) -> f
     """Whole-job units/s: every rank processes its own batch of units_per_rank
     (weak scaling), a step lasts as long as the slowest rank."""
     return world * units_per_rank / (ms_per_step_max * 1e-3)
+
+
+# --------------------------------------------------------------- our arm
+class Resident:
+    """A batch, its sample counts and positions and an output array, in HBM."""
+
+    def __init__(self, batch, dev):
+        import torch
+        tk = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)
+        self.batch = batch
+        self.arr = (tk(batch.kind, torch.uint8), tk(batch.degree, torch.uint8), tk(batch.dim, torch.uint8),
+                    tk(batch.knot_off, torch.int64), tk(batch.knots, torch.float64),
+                    tk(batch.ctrl_off, torch.int64), tk(batch.ctrl, torch.float64))
+        self.cnt = tk(batch.n_samples, torch.int32)
+        self.pos = tk(batch.positions, torch.float64)
+        self.out = torch.empty(batch.total_samples, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+
+
+class Bench:
+    """Device-resident timing of one batch: every call of the library, the
+    L2 flush and the CUDA events run on one stream of this object's own, so
+    the flush is ordered before each step and the events bracket it."""
+
+    def __init__(self, dev, local, dist, use_graph=True):
+        import torch
+        self.torch = torch
+        self.dev = dev
+        self.local = local
+        self.dist = dist
+        self.use_graph = use_graph
+        self.stream = torch.cuda.Stream(device=dev)
+        with torch.cuda.stream(self.stream):
+            self.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def run(self, res, prec, steps, warmup, learned_on=False, model=None, clocks=False):
+        """Times `steps` table builds + samplings (after `warmup` untimed ones)."""
+        import gcurval_gb300 as g
+        torch = self.torch
+        b = res.batch
+        with torch.cuda.stream(self.stream):
+            calc = g.ArclengthCalculateGpu.from_device_batch(*res.arr, precision=prec, rtol=b.rtol,
+                                                             collect_stats=True, learned=learned_on,
+                                                             stream=self.stream)
+            if learned_on:
+                calc.set_learned_model(model)
+
+            def step():
+                if self.use_graph:
+                    calc.stepGraph(res.cnt, res.pos, res.out, True, g.GCV_RETURN_US)
+                else:
+                    calc.createArclengthTable()
+                    calc.arclengthReverseInto(res.cnt, res.pos, res.out, True, g.GCV_RETURN_US)
+
+            for _ in range(warmup):
+                step()
+            self.stream.synchronize()
+            launches0 = calc.stats()["n_launches"]
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            r = {"ms_len": [], "ms_samp": [], "ms_setup": [], "n_newton": [], "n_panels": [], "ms_learned": []}
+            if self.dist:
+                self.dist.barrier()
+            torch.cuda.synchronize()
+            with ClockSampler(self.local) as clk:
+                for i in range(steps):
+                    self.flush.zero_()
+                    evs[i][0].record(self.stream)
+                    step()
+                    evs[i][1].record(self.stream)
+                    st = calc.stats()  # synchronises; outside the events
+                    r["ms_len"].append(st["ms_length"])
+                    r["ms_samp"].append(st["ms_sample"])
+                    r["ms_setup"].append(st["ms_setup"] + st["ms_scan"])
+                    r["n_newton"].append(st["n_newton"])
+                    r["n_panels"].append(st["n_panels"])
+                    r["ms_learned"].append(st["ms_learned"])
+                self.stream.synchronize()
+            if self.dist:
+                self.dist.barrier()
+            total_ms = max_over_ranks(float(sum(x.elapsed_time(y) for x, y in evs)), self.dist, self.dev)
+            st1 = calc.stats()
+            r["launches"] = st1["n_launches"] - launches0
+            r["leaves"] = st1["n_leaves"]
+            r["deep"] = st1["n_deep_segments"]
+            r["capped"] = st1["n_capped"]
+            r["ms_per_step"] = total_ms / steps
+            r["steps"] = steps
+            r["clocks"] = clk.summary() if clocks else None
+            calc.close()
+        return r
+
+
+def roofline_of(batch, r, plain_r, is_plain: bool, workload: str, precision: str, fp64_peak: float,
+                fp32_peak: float, hbm_peak):
+    """Roofline of the dominant phase of run r (the larger of length walk and
+    sampling).  achieved = the plain FP64 method's integrand evaluations for
+    the batch (plain_r's panels x 16 and Newton iterations x 9) x the
+    reference's FLOPs per evaluation, over the phase's time; the library's
+    own count (its own evaluations x its cheaper per-evaluation FLOPs) is
+    given beside it."""
+    n_samples = batch.total_samples
+    fpe = flops_per_eval(batch)
+    ms_inf = r["ms_learned"]
+    ms_l = float(np.mean([a - b for a, b in zip(r["ms_len"], ms_inf)]))
+    ms_s = float(np.mean(r["ms_samp"]))
+    newton, panels = float(np.mean(r["n_newton"])), float(np.mean(r["n_panels"]))
+    own_samp = newton * (8 * (fpe + 4.0) + fpe + 4.0) + n_samples * 20.0
+    own_len = panels * (16 * (fpe + 2.0) + 40.0)
+    src = plain_r if plain_r is not None else r
+    f_len = survey_flops_per_eval(batch, batch.n_segments)
+    f_smp = survey_flops_per_eval(batch, batch.n_samples)
+    sv_len = float(np.mean(src["n_panels"])) * 16.0 * f_len
+    sv_samp = float(np.mean(src["n_newton"])) * 9.0 * f_smp
+    if ms_s >= ms_l:
+        dom, flops, own, ms = "k_sample", sv_samp, own_samp, ms_s
+        bytes_alg = n_samples * (8 + 8 + 8) + batch.n_curve * 8
+        units = n_samples
+    else:
+        dom, flops, own, ms = "k_length", sv_len, own_len, ms_l
+        bytes_alg = batch.knots.nbytes + batch.ctrl.nbytes + int(batch.n_segments.sum()) * 8
+        units = float(batch.n_segments.sum())
+    peak = fp64_peak if is_plain else fp32_peak
+    achieved = flops / (ms * 1e-3) / 1e12
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic_per_unit.json")
+    if os.path.exists(prof):
+        try:
+            tpu = json.load(open(prof)).get(f"{dom}:{workload}:{precision}")
+            if tpu:
+                traffic = float(tpu) * units
+        except (ValueError, OSError):
+            traffic = None
+    return {
+        "kernel": dom, "bound": "fp64" if is_plain else "fp32",
+        "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+        "peak_source": "measured in-run by gcv_measure_fma_peak (FMA probe kernel)",
+        "work": ("evaluations of the plain FP64 method (panels x 16 + Newton iterations x 9) x FLOPs per "
+                 "evaluation of the reference's de Boor / ellipse derivative"),
+        "flops_per_eval_reference": round(f_smp if dom == "k_sample" else f_len, 3),
+        "traffic": traffic, "ms_per_launch": round(ms, 4), "algorithmic_flops_per_launch": flops,
+        "own_count": {"flops_per_eval": round(fpe, 3), "flops": own, "achieved": round(own / (ms * 1e-3) / 1e12, 4),
+                      "frac": round(own / (ms * 1e-3) / 1e12 / peak, 4),
+                      "work": "this form's own panels / Newton iterations x its FLOPs per evaluation"},
+        "hbm": {"achieved_gbs": round(bytes_alg / (ms * 1e-3) / 1e9, 2), "peak_gbs": hbm_peak,
+                "frac": round(bytes_alg / (ms * 1e-3) / 1e9 / hbm_peak, 4) if hbm_peak else None,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "phases_ms": {"length": round(ms_l, 4), "sample": round(ms_s, 4),
+                      "setup_scan": round(float(np.mean(r["ms_setup"])), 4),
+                      "network_inference": round(float(np.mean(ms_inf)), 4)},
+        "work_per_step": {"panels": panels, "newton_iterations": newton, "leaves": int(r["leaves"]),
+                          "segments": int(batch.n_segments.sum()), "capped_panels": int(r["capped"]),
+                          "plain_panels": float(np.mean(src["n_panels"])),
+                          "plain_newton_iterations": float(np.mean(src["n_newton"]))},
+        "fp64_peak_tflops": round(fp64_peak, 3), "fp32_peak_tflops": round(fp32_peak, 2),
+    }
+
+
+def hbm_peak_gbs():
+    mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(mp):
+        try:
+            return json.load(open(mp)).get("hbm_gbs")
+        except (ValueError, OSError):
+            return None
+    return None
+
+
+def measure_config(name, workload, precision, bench, args, fp64_peak, fp32_peak, nthreads):
+    """Value, roofline, accuracy and CPU baseline of one other workload."""
+    import gcurval_gb300 as g
+    batch = make_batch(workload, seed=0)
+    res = Resident(batch, bench.dev)
+    prec = g.GCV_PLAIN_FP64 if precision == "plain" else g.GCV_MIXED
+    r = bench.run(res, prec, args.config_steps, 3)
+    plain_r = None if precision == "plain" else bench.run(res, g.GCV_PLAIN_FP64, 2, 1)
+    del res
+    value = batch.n_curve / (r["ms_per_step"] * 1e-3)
+    out = {"workload": f"{workload}: {WORKLOADS[workload][1]}", "precision": precision, "rtol": batch.rtol,
+           "value": round(value, 3), "unit": "curves/s", "ms_per_step": round(r["ms_per_step"], 4),
+           "steps": r["steps"], "warmup": 3,
+           "samples_per_s": round(batch.total_samples / (r["ms_per_step"] * 1e-3), 1),
+           "roofline": roofline_of(batch, r, plain_r, precision == "plain", workload, precision, fp64_peak,
+                                   fp32_peak, hbm_peak_gbs())}
+    if plain_r is not None:
+        out["plain_fp64_same_batch"] = {"value": round(batch.n_curve / (plain_r["ms_per_step"] * 1e-3), 3),
+                                        "ms_per_step": round(plain_r["ms_per_step"], 4)}
+    if not args.no_accuracy:
+        sub = accuracy_subset(batch, 400, 40)
+        out["accuracy_vs_fp64_oracle"] = accuracy_vs_oracle(sub, {precision: (prec, False)}, batch.rtol)
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(batch, workload, nthreads)
+    return out
 
 
 def main():
@@ -269,131 +574,29 @@ def main():
     batch = make_batch(args.workload, seed=rank, n_curves=args.n_curves)
     pos = batch.positions
     n_curves, n_samples = batch.n_curve, batch.total_samples
+    rtol = batch.rtol
+    nthreads = os.cpu_count() or 1
 
     # ---- device-resident arm ------------------------------------------------
-    tk = lambda a, dt: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt)
-    d_arr = (tk(batch.kind, torch.uint8), tk(batch.degree, torch.uint8), tk(batch.dim, torch.uint8),
-             tk(batch.knot_off, torch.int64), tk(batch.knots, torch.float64), tk(batch.ctrl_off, torch.int64),
-             tk(batch.ctrl, torch.float64))
-    d_cnt = tk(batch.n_samples, torch.int32)
-    d_pos = tk(pos, torch.float64)
-    d_out = torch.empty(n_samples, dtype=torch.float64, device=dev)
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
-
-    def device_arm(prec, steps, warmup, clocks=False, learned_on=False):
-        """Times `steps` table builds + samplings of the resident batch with CUDA
-        events (L2 flushed before each); returns the per-step figures."""
-        calc = g.ArclengthCalculateGpu.from_device_batch(*d_arr, precision=prec, rtol=batch.rtol, collect_stats=True,
-                                                         learned=learned_on)
-        if learned_on:
-            calc.set_learned_model(model)
-
-        def step():
-            if use_graph:
-                calc.stepGraph(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
-            else:
-                calc.createArclengthTable()
-                calc.arclengthReverseInto(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
-
-        for _ in range(warmup):
-            step()
-        torch.cuda.synchronize()
-        launches0 = calc.stats()["n_launches"]
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-        r = {"ms_len": [], "ms_samp": [], "ms_setup": [], "n_newton": [], "n_panels": [], "ms_learned": []}
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-        with ClockSampler(local) as clk:
-            for i in range(steps):
-                flush.zero_()
-                evs[i][0].record()
-                step()
-                evs[i][1].record()
-                st = calc.stats()  # synchronises; outside the events
-                r["ms_len"].append(st["ms_length"])
-                r["ms_samp"].append(st["ms_sample"])
-                r["ms_setup"].append(st["ms_setup"] + st["ms_scan"])
-                r["n_newton"].append(st["n_newton"])
-                r["n_panels"].append(st["n_panels"])
-                r["ms_learned"].append(st["ms_learned"])
-            torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        total_ms = max_over_ranks(float(sum(x.elapsed_time(y) for x, y in evs)), dist, dev)
-        st1 = calc.stats()
-        r["launches"] = st1["n_launches"] - launches0
-        r["leaves"] = st1["n_leaves"]
-        r["deep"] = st1["n_deep_segments"]
-        r["ms_per_step"] = total_ms / steps
-        r["clocks"] = clk.summary() if clocks else None
-        calc.close()
-        return r
-
-    use_graph = not args.no_graph
-    main_r = device_arm(precision, args.steps, max(args.warmup, 3), clocks=True, learned_on=use_learned)
+    bench = Bench(dev, local, dist, use_graph=not args.no_graph)
+    res = Resident(batch, dev)
+    main_r = bench.run(res, precision, args.steps, max(args.warmup, 3), learned_on=use_learned, model=model,
+                       clocks=True)
     plain_r = mixed_r = None
     if precision != g.GCV_PLAIN_FP64 and args.plain_steps > 0:
-        plain_r = device_arm(g.GCV_PLAIN_FP64, args.plain_steps, 1)
+        plain_r = bench.run(res, g.GCV_PLAIN_FP64, args.plain_steps, 1)
         if use_learned:
             # the same mixed-precision walk without the network: what the network gains
-            mixed_r = device_arm(g.GCV_MIXED, args.plain_steps, 1)
+            mixed_r = bench.run(res, g.GCV_MIXED, args.plain_steps, 1)
+    del res
     ms_per_step = main_r["ms_per_step"]
-    launches = main_r["launches"]
-    leaves = main_r["leaves"]
-    ms_samp, n_newton, n_panels = main_r["ms_samp"], main_r["n_newton"], main_r["n_panels"]
-    ms_inf = main_r["ms_learned"]
-    ms_len = [a - b for a, b in zip(main_r["ms_len"], ms_inf)]  # the length passes without the network
     value = job_throughput(n_curves, ms_per_step, world)
     samples_per_s = world * n_samples / (ms_per_step * 1e-3)
-
-    # ---- accuracy of this run on a subset (vs the oracle) --------------------
-    # (reported, not asserted: tests/ carry the parity bars)
-    # ---- roofline of the dominant kernel ------------------------------------
-    fpe = flops_per_eval(batch)
-    samp_flops = float(np.mean(n_newton)) * (8 * (fpe + 4.0) + fpe + 4.0) + n_samples * 20.0
-    len_flops = float(np.mean(n_panels)) * (16 * (fpe + 2.0) + 40.0)
-    ms_s, ms_l = float(np.mean(ms_samp)), float(np.mean(ms_len))
     fp64_peak = _lib.measure_fma_peak(0)
     fp32_peak = _lib.measure_fma_peak(1)
-    if ms_s >= ms_l:
-        dom, flops, ms = "k_sample", samp_flops, ms_s
-        bytes_alg = n_samples * (8 + 8 + 8) + n_curves * 8
-    else:
-        dom, flops, ms = "k_length", len_flops, ms_l
-        bytes_alg = batch.knots.nbytes + batch.ctrl.nbytes + batch.n_segments.sum() * 8
-    achieved = flops / (ms * 1e-3) / 1e12
-    peak = fp64_peak if precision == g.GCV_PLAIN_FP64 else fp32_peak
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "traffic_per_unit.json")
-    if os.path.exists(prof):
-        try:
-            tpu = json.load(open(prof)).get(f"{dom}:{args.workload}:{args.precision}")
-            if tpu:
-                traffic = float(tpu) * (n_samples if dom == "k_sample" else float(batch.n_segments.sum()))
-        except (ValueError, OSError):
-            traffic = None
-    hbm_peak = None
-    mp = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    if os.path.exists(mp):
-        hbm_peak = json.load(open(mp)).get("hbm_gbs")
-    roofline = {
-        "kernel": dom, "bound": "fp64" if precision == g.GCV_PLAIN_FP64 else "fp32",
-        "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
-        "frac": round(achieved / peak, 4), "peak_source": "measured in-run by gcv_measure_fma_peak (FMA probe kernel)",
-        "traffic": traffic, "ms_per_launch": round(ms, 4), "algorithmic_flops_per_launch": flops,
-        "hbm": {"achieved_gbs": round(bytes_alg / (ms * 1e-3) / 1e9, 2), "peak_gbs": hbm_peak,
-                "frac": round(bytes_alg / (ms * 1e-3) / 1e9 / hbm_peak, 4) if hbm_peak else None,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
-        "phases_ms": {"length": round(ms_l, 4), "sample": round(ms_s, 4),
-                      "setup_scan": round(float(np.mean(main_r["ms_setup"])), 4),
-                      "network_inference": round(float(np.mean(ms_inf)), 4)},
-        "work_per_step": {"panels": float(np.mean(n_panels)), "newton_iterations": float(np.mean(n_newton)),
-                          "leaves": int(leaves), "segments": int(batch.n_segments.sum()),
-                          "length_tflops": round(len_flops / (ms_l * 1e-3) / 1e12, 4),
-                          "sample_tflops": round(samp_flops / (ms_s * 1e-3) / 1e12, 4)},
-        "fp32_peak_tflops": round(fp32_peak, 2),
-    }
+    roofline = roofline_of(batch, main_r, plain_r if precision != g.GCV_PLAIN_FP64 else None,
+                           precision == g.GCV_PLAIN_FP64, args.workload, args.precision, fp64_peak, fp32_peak,
+                           hbm_peak_gbs())
 
     # ---- end-to-end through the public API with host buffers -----------------
     e2e_t, parts = [], []
@@ -420,21 +623,37 @@ def main():
     h2d = batch.nbytes() + batch.n_samples.nbytes + pos.nbytes
     d2h = h_out.nbytes
 
-    # ---- CPU baseline and accuracy (rank 0, N = 1 only) ----------------------
+    # ---- accuracy, CPU baseline and the other configs (rank 0, N = 1 only) ---
     cpu = acc = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        nthreads = os.cpu_count() or 1
-        sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch, nthreads, 10.0))
-        secs, kind = run_cpu_reference(sub, nthreads)
-        cpu = {"value": round(sub.n_curve / secs, 3), "unit": "curves/s", "cores": nthreads, "kind": kind,
-               "sample": f"{sub.n_curve} curves of the workload ({sub.total_samples} samples), table + sampling, "
-                         f"{secs:.2f} s", "samples_per_s": round(sub.total_samples / secs, 1)}
-        acc = accuracy_vs_oracle(sub, precision, batch.rtol, model)
+    configs = None
+    if rank == 0 and world == 1:
+        if not args.no_accuracy:
+            sub = accuracy_subset(batch, 1000, 250)
+            forms = {args.precision: (precision, use_learned)}
+            if use_learned:
+                forms["mixed"] = (g.GCV_MIXED, False)
+            if precision != g.GCV_PLAIN_FP64:
+                forms["plain"] = (g.GCV_PLAIN_FP64, False)
+            acc = accuracy_vs_oracle(sub, forms, batch.rtol, model)
+            acc["subset"] = ("1,000 curves cost-stratified over the batch plus its hardest: the 250 with the most "
+                             "near-duplicate knots, the 250 degree-5 curves with the most, the 250 with the most "
+                             "knot intervals, the 250 with the most samples, 25 random curves of every code")
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(batch, args.workload, nthreads, args.cpu_sample_curves)
+        if not args.no_configs and args.workload == "uneven_batch" and not args.n_curves:
+            del batch
+            _lib.release_cached_memory()
+            torch.cuda.empty_cache()
+            configs = {}
+            for name, wl, pr in CONFIG_RUNS:
+                configs[name] = measure_config(name, wl, pr, bench, args, fp64_peak, fp32_peak, nthreads)
+                _lib.release_cached_memory()
+                torch.cuda.empty_cache()
     plain = None
     if plain_r is not None:
         pv = job_throughput(n_curves, plain_r["ms_per_step"], world)
         plain = {"value": round(pv, 3), "unit": "curves/s", "ms_per_step": round(plain_r["ms_per_step"], 4),
-                 "steps": args.plain_steps, "warmup": 1, "rtol": batch.rtol,
+                 "steps": args.plain_steps, "warmup": 1, "rtol": rtol,
                  "samples_per_s": round(world * n_samples / (plain_r["ms_per_step"] * 1e-3), 1),
                  "phases_ms": {"length": round(float(np.mean(plain_r["ms_len"])), 4),
                                "sample": round(float(np.mean(plain_r["ms_samp"])), 4),
@@ -443,38 +662,42 @@ def main():
     gain = None
     if mixed_r is not None:
         mv = job_throughput(n_curves, mixed_r["ms_per_step"], world)
+        ms_inf = main_r["ms_learned"]
         gain = {"mixed_without_network": {"value": round(mv, 3), "unit": "curves/s",
                                           "ms_per_step": round(mixed_r["ms_per_step"], 4),
                                           "panels": float(np.mean(mixed_r["n_panels"])),
                                           "length_ms": round(float(np.mean(mixed_r["ms_len"])), 4)},
-                "with_network": {"panels": float(np.mean(n_panels)), "length_ms": round(float(np.mean(ms_len)), 4),
+                "with_network": {"panels": float(np.mean(main_r["n_panels"])),
+                                 "length_ms": round(float(np.mean([a - b for a, b in zip(main_r["ms_len"], ms_inf)])), 4),
                                  "inference_ms": round(float(np.mean(ms_inf)), 4)},
-                "panels_saved_frac": round(1.0 - float(np.mean(n_panels)) / float(np.mean(mixed_r["n_panels"])), 4),
+                "panels_saved_frac": round(1.0 - float(np.mean(main_r["n_panels"])) / float(np.mean(mixed_r["n_panels"])), 4),
                 "speedup_over_mixed": round(value / mv, 4)}
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "curves/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == g.GCV_PLAIN_FP64 else ("f32+f64+bf16" if use_learned else "f32+f64"),
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if precision == g.GCV_PLAIN_FP64 else ("f32+f64+bf16" if use_learned else "f32+f64"),
             "data": "synthetic: seeded generator (numpy default_rng, seed = rank)",
             "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][1]}",
-                       "precision": args.precision, "rtol": batch.rtol,
+                       "precision": args.precision, "rtol": rtol,
                        "curves_per_gpu": n_curves, "samples_per_gpu": n_samples,
-                       "l2": "flushed between timed steps (256 MB write, untimed)",
-                       "step": "one captured CUDA graph per step (gcv_step_graph)" if use_graph else
+                       "l2": "flushed between timed steps (256 MB write on the step's stream, untimed)",
+                       "step": "one captured CUDA graph per step (gcv_step_graph)" if not args.no_graph else
                                "createArclengthTable + arclengthReverseInto",
                        "parallelism": f"replicas x{world} (independent curves, no collective)"},
             "samples_per_s": round(samples_per_s, 1),
             "e2e": {"value": round(world * n_curves / e2e_s, 3), "unit": "curves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "samples_per_s": round(world * n_samples / e2e_s, 1),
                     "ms_per_step": round(e2e_s * 1e3, 3), "breakdown_ms": e2e_parts},
-            "gpu_launches": int(launches),
+            "gpu_launches": int(main_r["launches"]),
             "roofline": roofline,
             "cpu_baseline": cpu,
             "accuracy_vs_fp64_oracle": acc,
             "plain_fp64_same_batch": plain,
             "learned_gain": gain,
+            "configs": configs,
             "clocks": main_r["clocks"],
         }
         print(json.dumps(line), flush=True)
@@ -483,29 +706,35 @@ def main():
 
 
 def reference_arm(args):
+    """The reference's CPU implementation of the path on this host's cores:
+    each step one pass (table + sampling) over the same cost-stratified
+    sample the cpu_baseline leg times, all host threads, the reference's
+    default tolerance."""
     nthreads = os.cpu_count() or 1
     batch = make_batch(args.workload, seed=0, n_curves=args.n_curves)
-    # each step a bounded sample: the whole --steps / --warmup run stays within minutes
-    per_step_s = min(5.0, 150.0 / max(args.steps + max(args.warmup, 3), 1))
-    sub = cpu_sample(batch, args.cpu_sample_curves or auto_cpu_curves(batch, nthreads, per_step_s))
+    sub = cpu_sample(batch, args.cpu_sample_curves or CPU_SAMPLES[args.workload]["default"][0])
     times, kind = [], None
     for i in range(max(args.warmup, 3) + args.steps):
-        secs, kind = run_cpu_reference(sub, nthreads)
+        secs, kind = run_cpu_reference(sub, nthreads, REF_MAX_ERROR)
         if i >= max(args.warmup, 3):
             times.append(secs)
     per = float(np.mean(times))
     value = sub.n_curve / per
+    nseg = int(sub.n_segments.sum())
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "curves/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": round(per * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: seeded generator (numpy default_rng, seed 0)",
         "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][1]}", "precision": "plain",
-                   "sample_curves": sub.n_curve},
+                   "sample_curves": sub.n_curve, "max_error": REF_MAX_ERROR},
         "samples_per_s": round(sub.total_samples / per, 1),
+        "intervals_per_s": round(nseg / per, 1),
         "cpu_baseline": {"value": round(value, 3), "unit": "curves/s", "cores": nthreads, "kind": kind,
-                         "sample": f"{sub.n_curve} curves of the workload ({sub.total_samples} samples) per step, "
-                                   "table + sampling, all host threads"},
+                         "sample": f"{sub.n_curve} curves, a cost-stratified sample of the workload "
+                                   f"({sub.total_samples} samples, {nseg} knot intervals) per step, table + "
+                                   f"sampling, all host threads, absolute tolerance {REF_MAX_ERROR:g}",
+                         "cpu_model": cpu_model(), "nproc": os.cpu_count()},
         "e2e": {"value": round(value, 3), "unit": "curves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

@@ -299,6 +299,95 @@ def uneven_batch(n: int = 1_000_000, seed: int = 0, rtol: float = 5e-9,
     return _pack(kind, deg, dm, klen, knots, clen, ctrl, n_samp, "uneven_batch", rtol)
 
 
+# ------------------------------------------------------------ subsets
+def cost_proxy(batch: CurveBatch) -> np.ndarray:
+    """A per-curve work estimate for stratified sampling: knot intervals
+    (weighted as the tens of integrand evaluations each costs) plus samples."""
+    return 32.0 * batch.n_segments.astype(np.float64) + batch.n_samples.astype(np.float64)
+
+
+def stratified_indices(batch: CurveBatch, n: int) -> np.ndarray:
+    """n curves spread evenly over the batch sorted by cost_proxy (a
+    systematic sample of the cost distribution: its mean cost matches the
+    batch's far more closely than a uniform sample of the same size when
+    costs are heavy-tailed).  Sorted by descending cost."""
+    n = int(min(max(n, 0), batch.n_curve))
+    if n == 0:
+        return np.zeros(0, np.int64)
+    cost = cost_proxy(batch)
+    order = np.argsort(cost, kind="stable")
+    pick = order[((np.arange(n) + 0.5) * batch.n_curve / n).astype(np.int64)]
+    return pick[np.argsort(-cost[pick], kind="stable")]
+
+
+def near_duplicate_knots(batch: CurveBatch, gap: float = 1e-5) -> np.ndarray:
+    """Per curve, the number of consecutive knot pairs closer than `gap`
+    but not equal (the uneven batch's near-duplicate knots)."""
+    d = np.diff(batch.knots)
+    close = (d > 0.0) & (d < gap)
+    # pairs that cross a curve boundary do not count
+    ends = batch.knot_off[1:-1] - 1
+    close[ends[(ends >= 0) & (ends < close.size)]] = False
+    cnt = np.zeros(batch.n_curve, np.int64)
+    if close.size:
+        owner = np.searchsorted(batch.knot_off, np.nonzero(close)[0], side="right") - 1
+        np.add.at(cnt, owner, 1)
+    return cnt
+
+
+def hard_case_indices(batch: CurveBatch, k: int = 200, seed: int = 0) -> np.ndarray:
+    """The curves where accuracy is hardest to hold, for the accuracy checks:
+    the k with the most near-duplicate knots, the k degree-5 curves with the
+    most near-duplicate knots, the k with the most knot intervals, the k with
+    the most samples, and k / 10 random curves of every curve code."""
+    rng = np.random.default_rng(seed)
+    dup = near_duplicate_knots(batch)
+    nseg = batch.n_segments
+    parts = [np.argsort(-dup, kind="stable")[:k]]
+    d5 = np.nonzero((batch.kind == KIND_BSPLINE) & (batch.degree == 5))[0]
+    parts.append(d5[np.argsort(-dup[d5], kind="stable")[:k]])
+    parts.append(np.argsort(-nseg, kind="stable")[:k])
+    parts.append(np.argsort(-batch.n_samples.astype(np.int64), kind="stable")[:k])
+    code = np.where(batch.kind == KIND_ELLIPSE, -1, batch.degree.astype(np.int64) * 10 + batch.dim)
+    for c in np.unique(code):
+        idx = np.nonzero(code == c)[0]
+        parts.append(rng.choice(idx, size=min(idx.size, max(1, k // 10)), replace=False))
+    return np.unique(np.concatenate(parts))
+
+
+def accuracy_subset_indices(batch: CurveBatch, n_stratified: int = 1000, k_hard: int = 250) -> np.ndarray:
+    """A stratified sample of the batch plus its hard cases (sorted indices)."""
+    return np.union1d(stratified_indices(batch, n_stratified), hard_case_indices(batch, k_hard))
+
+
+def control_polygon_length(batch: CurveBatch) -> np.ndarray:
+    """Per curve, the length of the control polygon (B-splines; an upper
+    bound of the curve's length) or 2 pi max(a, b) (ellipses)."""
+    out = np.zeros(batch.n_curve)
+    ell = np.nonzero(batch.kind == KIND_ELLIPSE)[0]
+    if ell.size:
+        a = batch.ctrl[batch.ctrl_off[ell]]
+        b = batch.ctrl[batch.ctrl_off[ell] + 1]
+        out[ell] = TWO_PI * np.maximum(np.abs(a), np.abs(b))
+    for d in (2, 3):
+        sel = np.nonzero((batch.kind == KIND_BSPLINE) & (batch.dim == d))[0]
+        if not sel.size:
+            continue
+        npts = (batch.ctrl_off[sel + 1] - batch.ctrl_off[sel]) // d
+        idx = _ragged_index(batch.ctrl_off[sel], npts * d)
+        pts = batch.ctrl[idx].reshape(-1, d)
+        seg = np.linalg.norm(np.diff(pts, axis=0), axis=1)
+        first = np.concatenate([[0], np.cumsum(npts)[:-1]])
+        # drop the steps that join consecutive curves
+        keep = np.ones(seg.size, bool)
+        keep[(first[1:] - 1)] = False
+        owner = np.repeat(np.arange(sel.size), npts)[1:]
+        tot = np.zeros(sel.size)
+        np.add.at(tot, owner[keep], seg[keep])
+        out[sel] = tot
+    return out
+
+
 WORKLOADS = {
     "ellipses": ellipses,
     "uniform_bsplines": uniform_bsplines,

@@ -58,10 +58,17 @@ typedef struct pack {
     uint64_t* evals;
 } pack_t;
 
-static void bspline_deriv(double u, const pack_t* pk, double* out)
+/* The de Boor routines below take the degree p and dimension d as
+ * arguments of always-inlined bodies; the dispatchers after them call the
+ * bodies with constant (p, d), so each common case is compiled with its
+ * loops unrolled, as the reference's degree-templated functions are
+ * (same operations in the same order: the results do not change). */
+#define GCVO_INLINE static inline __attribute__((always_inline))
+
+GCVO_INLINE void bspline_deriv_pd(double u, const pack_t* pk, double* out, const int p, const int d)
 {
     double f[9], left[9], right[9], saved, temp;
-    const int p = pk->p, span = pk->span;
+    const int span = pk->span;
     const double* kv = pk->kv;
     f[0] = 1.0;
     for (int j = 1; j < p; j++) {
@@ -84,17 +91,16 @@ static void bspline_deriv(double u, const pack_t* pk, double* out)
         saved = temp;
     }
     f[p] = saved;
-    const int d = pk->dim;
     const double* c0 = pk->cp + (size_t)(span - p) * d;
     for (int k = 0; k < d; k++) out[k] = c0[k] * f[0];
     for (int i = 1; i <= p; i++)
         for (int k = 0; k < d; k++) out[k] += c0[(size_t)i * d + k] * f[i];
 }
 
-static void bspline_point(double u, const pack_t* pk, double* out)
+GCVO_INLINE void bspline_point_pd(double u, const pack_t* pk, double* out, const int p, const int d)
 {
     double f[9], left[9], right[9], saved, temp;
-    const int p = pk->p, span = pk->span;
+    const int span = pk->span;
     const double* kv = pk->kv;
     f[0] = 1.0;
     for (int j = 1; j <= p; j++) {
@@ -108,27 +114,56 @@ static void bspline_point(double u, const pack_t* pk, double* out)
         }
         f[j] = saved;
     }
-    const int d = pk->dim;
     const double* c0 = pk->cp + (size_t)(span - p) * d;
     for (int k = 0; k < d; k++) out[k] = c0[k] * f[0];
     for (int i = 1; i <= p; i++)
         for (int k = 0; k < d; k++) out[k] += c0[(size_t)i * d + k] * f[i];
 }
 
-static double speed(const pack_t* pk, double u)
+#define GCVO_PD_CASES(FN)                                                                        \
+    case 1 * 4 + 2: FN(1, 2); return;                                                            \
+    case 2 * 4 + 2: FN(2, 2); return;                                                            \
+    case 3 * 4 + 2: FN(3, 2); return;                                                            \
+    case 4 * 4 + 2: FN(4, 2); return;                                                            \
+    case 5 * 4 + 2: FN(5, 2); return;                                                            \
+    case 1 * 4 + 3: FN(1, 3); return;                                                            \
+    case 2 * 4 + 3: FN(2, 3); return;                                                            \
+    case 3 * 4 + 3: FN(3, 3); return;                                                            \
+    case 4 * 4 + 3: FN(4, 3); return;                                                            \
+    case 5 * 4 + 3: FN(5, 3); return;
+
+static void bspline_point(double u, const pack_t* pk, double* out)
+{
+#define GCVO_P(P, D) bspline_point_pd(u, pk, out, P, D)
+    switch (pk->p * 4 + pk->dim) {
+        GCVO_PD_CASES(GCVO_P)
+    default: bspline_point_pd(u, pk, out, pk->p, pk->dim); return;
+    }
+#undef GCVO_P
+}
+
+GCVO_INLINE double speed_pd(const pack_t* pk, double u, const int p, const int d)
 {
     double v[3] = {0.0, 0.0, 0.0}, s = 0.0;
-    (*pk->evals)++;
-    if (pk->kind == 0) {
-        v[0] = -1.0 * pk->cp[0] * sin(u);
-        v[1] = pk->cp[1] * cos(u);
-        s = v[0] * v[0];
-        s += v[1] * v[1];
-        return sqrt(s);
-    }
-    bspline_deriv(u, pk, v);
-    for (int k = 0; k < pk->dim; k++) s += v[k] * v[k];
+    bspline_deriv_pd(u, pk, v, p, d);
+    for (int k = 0; k < d; k++) s += v[k] * v[k];
     return sqrt(s);
+}
+
+GCVO_INLINE double ellipse_speed(const pack_t* pk, double u)
+{
+    double v[2], s;
+    v[0] = -1.0 * pk->cp[0] * sin(u);
+    v[1] = pk->cp[1] * cos(u);
+    s = v[0] * v[0];
+    s += v[1] * v[1];
+    return sqrt(s);
+}
+
+static double speed(const pack_t* pk, double u)
+{
+    if (pk->kind == 0) return ellipse_speed(pk, u);
+    return speed_pd(pk, u, pk->p, pk->dim);
 }
 
 static void point(const pack_t* pk, double u, double* out)
@@ -144,14 +179,40 @@ static void point(const pack_t* pk, double u, double* out)
     bspline_point(u, pk, out);
 }
 
+/* GaussLegendreQuadrature with 3 nodes (gcurval/base/functors.inl.h:39-66);
+ * the speed of each node is inlined for the curve's (p, d). */
+#define GCVO_GL3_BODY(SPEED)                                                                     \
+    do {                                                                                         \
+        for (int j = 0; j < 3; j++) {                                                            \
+            const double u = k * GL3_X[j] + b;                                                   \
+            acc += GL3_W[j] * (SPEED);                                                           \
+        }                                                                                        \
+    } while (0)
+
 static double gl3(const pack_t* pk, double begin, double end)
 {
     const double k = (end - begin) / 2.0;
     const double b = (end + begin) / 2.0;
     double acc = 0.0;
-    for (int j = 0; j < 3; j++) {
-        const double u = k * GL3_X[j] + b;
-        acc += GL3_W[j] * speed(pk, u);
+    *pk->evals += 3;
+    if (pk->kind == 0) {
+        GCVO_GL3_BODY(ellipse_speed(pk, u));
+    } else {
+#define GCVO_G(P, D) GCVO_GL3_BODY(speed_pd(pk, u, P, D)); break
+        switch (pk->p * 4 + pk->dim) {
+        case 1 * 4 + 2: GCVO_G(1, 2);
+        case 2 * 4 + 2: GCVO_G(2, 2);
+        case 3 * 4 + 2: GCVO_G(3, 2);
+        case 4 * 4 + 2: GCVO_G(4, 2);
+        case 5 * 4 + 2: GCVO_G(5, 2);
+        case 1 * 4 + 3: GCVO_G(1, 3);
+        case 2 * 4 + 3: GCVO_G(2, 3);
+        case 3 * 4 + 3: GCVO_G(3, 3);
+        case 4 * 4 + 3: GCVO_G(4, 3);
+        case 5 * 4 + 3: GCVO_G(5, 3);
+        default: GCVO_GL3_BODY(speed_pd(pk, u, pk->p, pk->dim)); break;
+        }
+#undef GCVO_G
     }
     acc *= k;
     return acc;
@@ -194,6 +255,7 @@ struct gcvo_table {
     const gcvo_batch* b;
     gcvo_batch bcopy;
     double max_error;
+    double eps[64]; /* max_error * 2^-level, as the reference's per-level table */
     int max_depth;
     curve_tab* tabs;
     double* length;
@@ -215,7 +277,7 @@ static void tab_push(curve_tab* t, double u, double al, int seg)
     t->n++;
 }
 
-static double eps_at(const gcvo_table* t, int level) { return ldexp(t->max_error, -level); }
+static double eps_at(const gcvo_table* t, int level) { return t->eps[level]; }
 
 /* arclengthRecursive: total_length is the length accumulated inside the
  * segment up to `begin` (passed by value, as in the reference). */
@@ -342,6 +404,7 @@ gcvo_table* gcvo_build(const gcvo_batch* batch, double max_error, int max_depth,
     t->b = &t->bcopy;
     t->max_error = max_error;
     t->max_depth = max_depth;
+    for (int k = 0; k < 64; k++) t->eps[k] = ldexp(max_error, -k);
     t->tabs = (curve_tab*)calloc((size_t)(batch->n_curve > 0 ? batch->n_curve : 1), sizeof(curve_tab));
     t->length = (double*)calloc((size_t)(batch->n_curve > 0 ? batch->n_curve : 1), sizeof(double));
     pthread_mutex_init(&t->lock, NULL);

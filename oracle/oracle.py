@@ -183,6 +183,48 @@ class Oracle:
                 np.ctypeslib.as_array(sg, (n,)).copy())
 
 
+class ScaledOracle:
+    """The oracle with its absolute tolerance scaled per curve: max_error =
+    rel x the curve's control-polygon length (a bound of its length), rounded
+    down to a power of two; curves of one tolerance share one Oracle.  The
+    reference's fixed absolute tolerance (1e-14) makes curves thousands of
+    units long refine to its depth limit at great cost without need; at
+    rel = 1e-16 every length is good to ~1e-14 relative, far below the 1e-8
+    the GPU forms are checked against.  Same algorithm, only MAX_ERROR differs
+    per group (a compile-time constant of the reference)."""
+
+    def __init__(self, batch, rel: float = 1e-16, nthreads: int | None = None):
+        from gcurval_gb300 import datasets as ds
+        self.batch = batch
+        pl = ds.control_polygon_length(batch)
+        tol = np.exp2(np.floor(np.log2(np.maximum(rel * pl, 1e-300))))
+        self.groups = []
+        for t in np.unique(tol):
+            idx = np.nonzero(tol == t)[0]
+            sub = batch.subset(idx)
+            self.groups.append((idx, sub, Oracle(sub, max_error=float(max(t, 1e-300)), nthreads=nthreads)))
+
+    def lengths(self) -> np.ndarray:
+        out = np.zeros(self.batch.n_curve)
+        for idx, _, o in self.groups:
+            out[idx] = o.lengths()
+        return out
+
+    def s_at(self, n_per_curve, u) -> np.ndarray:
+        """Arc length from each curve's start to each u (curve-major, as the
+        batch orders its samples)."""
+        n = np.ascontiguousarray(n_per_curve, np.int64)
+        u = np.ascontiguousarray(u, np.float64)
+        off = np.concatenate([[0], np.cumsum(n)])
+        if off[-1] != u.size:
+            raise ValueError("sample counts do not match the number of values")
+        out = np.zeros(u.size)
+        for idx, _, o in self.groups:
+            sel = np.concatenate([np.arange(off[i], off[i + 1]) for i in idx]) if idx.size else np.zeros(0, np.int64)
+            out[sel] = o.s_at(n[idx].astype(np.int32), u[sel])
+        return out
+
+
 _ref = None
 
 

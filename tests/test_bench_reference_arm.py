@@ -11,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_reference_arm_prints_the_contract_line():
-    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--n-curves", "2000", "--steps", "1",
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--n-curves", "2000", "--cpu-sample-curves", "64", "--steps", "1",
                         "--warmup", "1"], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     d = json.loads(r.stdout.strip().splitlines()[-1])
