@@ -182,8 +182,17 @@ __device__ __forceinline__ double speed_slope_of(int code, const double* r, doub
 // from the guess vg: F(v) = S(v) - rr with S(v) = S(va) + GL8(va, v) or
 // S(vb) - GL8(v, vb), whichever side of v is shorter (at most half a leaf,
 // where GL8 is far more accurate than the leaf's own G7 error estimate);
-// bracketed by bisection.  Stops once the residual after the step,
-// about |f'(v)| dn^2 / 2, is below eps_s.
+// bracketed by bisection.
+// Each iteration takes a second-order step: with f0 = f(v) and f1 = f(v - dn)
+// at the Newton point (dn = F / f0), the trapezoid rule d (f0 + f1) / 2
+// gives the arc length of a step d, so d = 2 F / (f0 + f1).  It stops when
+// that step's residual is below eps_s: the trapezoid error |d|^3 |f''| / 12
+// with f'' from the two slopes, taken 4-fold (dn^2 |f'(v - dn) - f'(v)| / 3),
+// plus |f'|^2 |dn|^3 / (4 f) for using f at v - dn rather than at v - d.
+// A first-order test from the slope at v alone (|f'(v)| dn^2 / 2) accepts
+// large steps wherever v sits at an extremum of the speed (f'(v) ~ 0), and
+// misplaced such samples by 1e-8 of the curve's length; this test sees the
+// slope change across the step.
 // 8-point Gauss nodes (-x0..-x3, x0..x3) and weights w0..w3 for rolled loops
 static __constant__ double c_gl8[12] = {-gl8_x(0), -gl8_x(1), -gl8_x(2), -gl8_x(3), gl8_x(0), gl8_x(1),
                                         gl8_x(2),  gl8_x(3),  gl8_w(0),  gl8_w(1),  gl8_w(2), gl8_w(3)};
@@ -222,14 +231,26 @@ __device__ __forceinline__ double leaf_newton(const double* __restrict__ seg, do
             blo = v;
         else
             bhi = v;
-        double qv;
-        const double fv = Eval<C>::speed_slope(r, v, qv);
-        const double dn = F / fv;
-        if (0.5 * fabs(qv) * dn * dn <= eps_s * fv) {  // converged after this step
-            v = fmin(fmax(v - dn, va), vb);
-            break;
-        }
+        double q0;
+        const double f0 = Eval<C>::speed_slope(r, v, q0);
+        const double dn = F / f0;
         double vn = v - dn;
+        // the second-order step only from a Newton point inside the closed
+        // bracket (a step below one ulp of v leaves vn == v, which must still
+        // converge); a Newton point outside it would take f1 from the
+        // polynomial extrapolated past the leaf
+        if (vn >= blo && vn <= bhi) {
+            double q1;
+            const double f1 = Eval<C>::speed_slope(r, vn, q1);
+            const double d = 2.0 * F / (f0 + f1);
+            const double s0 = q0 / f0, s1 = q1 / f1;  // f'(v), f'(v - dn)
+            const double res = dn * dn * (fabs(s1 - s0) * (1.0 / 3.0) + s1 * s1 * fabs(dn) / (4.0 * f1));
+            vn = v - d;
+            if (res <= eps_s && vn >= va && vn <= vb) {  // converged with this step
+                v = vn;
+                break;
+            }
+        }
         if (!(vn > blo && vn < bhi)) vn = 0.5 * (blo + bhi);  // safeguard (also NaN)
         v = vn;
     }
@@ -302,9 +323,8 @@ __global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample(SampleParams P)
                     vg = fmin(fmax(vg, va), vb);
                 }
                 const double* seg = t.coef + b.coef_off[c] + (s - s0) * code_stride(code);
-                // After a Newton step dn from v the residual is about |f'(v)| dn^2 / 2;
-                // stop when that is below 1 % of the sample tolerance rtol * L
-                // (tested as |q| dn^2 / 2 <= eps_s f, with q = f f', no division).
+                // stop when the residual of the last step is below 1 % of the
+                // sample tolerance rtol * L
                 const double eps_s = 0.01 * P.rtol * L;
                 if constexpr (CODE >= 0) {
                     v = leaf_newton<(CODE >= 0 ? CODE : 0)>(seg, va, vb, base, cb, rr, vg, eps_s, newton);

@@ -23,6 +23,9 @@ namespace gcv {
 // Newton on one leaf in float-float, in the local offset w = v - va in
 // [0, dv]: F(w) = S(va + w) - S(va) - rl with the partial integral taken by
 // 8-point Gauss over the shorter side of the leaf, bracketed by bisection.
+// Second-order steps and the stopping test of leaf_newton (gcv_kernels.cuh):
+// d = 2 F / (f0 + f1) with f1 the speed at the Newton point, stop when
+// dn^2 (|f'(w - dn) - f'(w)| / 3 + |f'|^2 |dn| / (4 f)) <= eps_s.
 // Returns the final offset, whose last update is done in FP64.
 // 8-point Gauss nodes (-x0..-x3, x0..x3) then weights w0..w3, float-float
 #define GCV_FFC(x) {split_const(x).hi, split_const(x).lo}
@@ -75,18 +78,33 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
             blo = w.hi;
         else
             bhi = w.hi;
-        float qv;
-        const ff fv = EvalFF<C>::speed_slope(r, ff_add(vaf, w), qv);
-        const float dn = Fh / fv.hi;
-        if (0.5f * fabsf(qv) * dn * dn <= eps_s * fv.hi) {
-            last = dn;  // converged
-            break;
-        }
+        float q0;
+        const float f0 = EvalFF<C>::speed_slope(r, ff_add(vaf, w), q0).hi;
+        const float dn = Fh / f0;
+        float step = dn;
+        // the second-order step only from a Newton point inside the closed
+        // bracket (a step below one FP32 ulp of w leaves w.hi - dn == w.hi,
+        // which must still converge); a Newton point outside it would take
+        // f1 from the polynomial extrapolated past the leaf
         const float wn = w.hi - dn;
-        if (!(wn > blo && wn < bhi))
-            w = ff{0.5f * (blo + bhi), 0.0f};  // safeguard (also NaN)
+        if (wn >= blo && wn <= bhi) {
+            float q1;
+            const float f1 = EvalFF<C>::speed_slope(r, ff_add(vaf, ff_add_f(w, -dn)), q1).hi;
+            const float d = 2.0f * Fh / (f0 + f1);
+            const float s0 = q0 / f0, s1 = q1 / f1;  // f'(w), f'(w - dn)
+            const float res = dn * dn * (fabsf(s1 - s0) * (1.0f / 3.0f) + s1 * s1 * fabsf(dn) / (4.0f * f1));
+            const float wd = w.hi - d;
+            if (res <= eps_s && wd >= 0.0f && wd <= dv) {
+                last = d;  // converged: the step is applied in FP64
+                break;
+            }
+            step = d;
+        }
+        const float ws = w.hi - step;
+        if (ws > blo && ws < bhi)
+            w = ff_add_f(w, -step);
         else
-            w = ff_add_f(w, -dn);
+            w = ff{0.5f * (blo + bhi), 0.0f};  // safeguard (also NaN)
     }
     // the final update in FP64
     return ((double)w.hi + (double)w.lo) - (double)last;
