@@ -293,6 +293,118 @@ __device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, 
     G = ff_scale(gg, hw);
 }
 
+// B-spline panels by node pairs.  The speed polynomials p_d (degree P - 1 in
+// v) are shifted to the panel's midpoint m and scaled to its half width h:
+// b_j = h^j p_d^(j)(m) / j!, so p_d(m + h x) = sum_j b_j x^j on x in [-1, 1]
+// (Horner-form Taylor shift, (P - 1) P / 2 float-float FMAs per dimension,
+// then exact power-of-two scaling; on deep panels the high terms may
+// underflow, where they are below any float-float rounding of b_0).  The
+// symmetric nodes m -+ h x_i then share one evaluation of the even part
+// E = b_0 + b_2 x^2 + ... and the odd part O = x (b_1 + b_3 x^2 + ...):
+// p(m -+ h x) = E -+ O.  Per pair of nodes this replaces two Horner passes
+// in v (2 (P - 1) float-float FMAs per dimension) and the two node
+// positions by about half the work; K15 and G7 are formed as in
+// panel_k15_ff.
+#define GCV_FFC2(x) {split_const(x).hi, split_const(x).lo}
+static __constant__ float2 c_gk_x2_ff[7] = {
+    GCV_FFC2(gk_x(0) * gk_x(0)), GCV_FFC2(gk_x(1) * gk_x(1)), GCV_FFC2(gk_x(2) * gk_x(2)),
+    GCV_FFC2(gk_x(3) * gk_x(3)), GCV_FFC2(gk_x(4) * gk_x(4)), GCV_FFC2(gk_x(5) * gk_x(5)),
+    GCV_FFC2(gk_x(6) * gk_x(6))};
+#undef GCV_FFC2
+
+template <int P, int D>
+__device__ __forceinline__ void ff_node_pair(const ff* b, ff x, ff x2, ff& fm, ff& fp)
+{
+    constexpr int N = P - 1;                       // polynomial degree
+    constexpr int JE = (N % 2 == 0) ? N : N - 1;   // highest even power
+    constexpr int JO = (N % 2 == 1) ? N : N - 1;   // highest odd power (-1: none)
+    ff sm{0.0f, 0.0f}, sp{0.0f, 0.0f};
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        ff e = b[JE * D + d];
+#pragma unroll
+        for (int j = JE - 2; j >= 0; j -= 2) e = ff_fma(e, x2, b[j * D + d]);
+        ff lo_ = e, hi_ = e;
+        if constexpr (JO >= 1) {
+            ff o = b[JO * D + d];
+#pragma unroll
+            for (int j = JO - 2; j >= 1; j -= 2) o = ff_fma(o, x2, b[j * D + d]);
+            o = ff_mul(o, x);
+            lo_ = ff_add(e, ff_neg(o));
+            hi_ = ff_add(e, o);
+        }
+        sm = d == 0 ? ff_mul(lo_, lo_) : ff_fma(lo_, lo_, sm);
+        sp = d == 0 ? ff_mul(hi_, hi_) : ff_fma(hi_, hi_, sp);
+    }
+    fm = ff_sqrt(sm);
+    fp = ff_sqrt(sp);
+}
+
+// b: the interval's speed coefficients on entry, shifted in place
+template <int CODE>
+__device__ __forceinline__ void panel_k15_ff_pairs(ff* b, unsigned long long k, int depth, ff& K, ff& G)
+{
+    constexpr int P = code_degree(CODE), D = code_dim(CODE);
+    const float hw = __int_as_float((127 - depth) << 23);  // 2^-depth, exact
+    const float kh = (float)(unsigned)(k >> 24), kl = (float)(unsigned)(k & 0xFFFFFFull);
+    const float sh = __int_as_float((127 + 25 - depth) << 23), sl = 2.0f * hw;  // 2^(25-depth), 2^(1-depth)
+    const ff vlo = ff_add_f(two_sum(-1.0f, kh * sh), kl * sl);
+    const ff mid = ff_add_f(vlo, hw);
+    // Taylor shift to mid: after pass i, b[i] holds p^(i)(mid) / i!
+#pragma unroll
+    for (int i = 0; i < P - 1; ++i)
+#pragma unroll
+        for (int j = P - 2; j >= i; --j)
+#pragma unroll
+            for (int d = 0; d < D; ++d) b[j * D + d] = ff_fma(b[(j + 1) * D + d], mid, b[j * D + d]);
+    float sc = hw;
+#pragma unroll
+    for (int j = 1; j < P; ++j) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) b[j * D + d] = ff_scale(b[j * D + d], sc);
+        sc *= hw;
+    }
+    ff s0{0.0f, 0.0f};
+#pragma unroll
+    for (int d = 0; d < D; ++d) s0 = d == 0 ? ff_mul(b[d], b[d]) : ff_fma(b[d], b[d], s0);
+    const ff fc = ff_sqrt(s0);
+    ff kk = ff_mul(to_ff(split_const(gk_wk(7))), fc);
+    ff gg = ff_mul(to_ff(split_const(gk_wg(7))), fc);
+    if constexpr (panel_rolled<CODE>()) {
+#pragma unroll 1
+        for (int i = 0; i < 7; ++i) {
+            ff fm, fp;
+            ff_node_pair<P, D>(b, ff{c_gk_ff[i].x, c_gk_ff[i].y}, ff{c_gk_x2_ff[i].x, c_gk_x2_ff[i].y}, fm, fp);
+            const ff sum = ff_add(fm, fp);
+            kk = ff_fma(ff{c_gk_ff[7 + i].x, c_gk_ff[7 + i].y}, sum, kk);
+            gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, sum, gg);  // weight 0 on Kronrod-only nodes
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+            ff fm, fp;
+            ff_node_pair<P, D>(b, to_ff(split_const(gk_x(i))), to_ff(split_const(gk_x(i) * gk_x(i))), fm, fp);
+            const ff sum = ff_add(fm, fp);
+            kk = ff_fma(to_ff(split_const(gk_wk(i))), sum, kk);
+            if (i & 1) gg = ff_fma(to_ff(split_const(gk_wg(i))), sum, gg);
+        }
+    }
+    K = ff_scale(kk, hw);
+    G = ff_scale(gg, hw);
+}
+
+// the float-float panel of a curve code: node pairs for B-splines, node by
+// node for the ellipse's sin(pi x) integrand; r (the interval's speed
+// coefficients) is scratch: the B-spline panel shifts it in place
+template <int CODE>
+__device__ __forceinline__ void panel_ff(ff* r, unsigned long long k, int depth, ff& K, ff& G)
+{
+    if constexpr (CODE == 0)
+        panel_k15_ff<CODE>(r, k, depth, K, G);
+    else
+        panel_k15_ff_pairs<CODE>(r, k, depth, K, G);
+}
+
 __device__ __forceinline__ void load_ff_dyn(int code, const float2* __restrict__ seg, ff* r)
 {
     switch (code) {
@@ -304,11 +416,11 @@ __device__ __forceinline__ void load_ff_dyn(int code, const float2* __restrict__
     }
 }
 
-__device__ __forceinline__ void panel_ff_dyn(int code, const ff* r, unsigned long long k, int depth, ff& K, ff& G)
+__device__ __forceinline__ void panel_ff_dyn(int code, ff* r, unsigned long long k, int depth, ff& K, ff& G)
 {
     switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: panel_k15_ff<C>(r, k, depth, K, G); break;
+    case C: panel_ff<C>(r, k, depth, K, G); break;
         GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
     default: K = G = ff{0.0f, 0.0f}; break;

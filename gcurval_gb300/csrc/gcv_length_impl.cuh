@@ -106,7 +106,10 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
     int64_t s = 0, pool = 0;
     int code = CODE >= 0 ? CODE : 0;
     double r[PREC == 0 ? MAX_COEF : 1];
-    ff rf[PREC == 1 ? MAX_COEF : 1];
+    // float-float path: the interval's coefficients are reloaded for every
+    // panel (L1 hits) rather than kept in registers: the panel shifts its
+    // copy in place, and the registers go to occupancy
+    const float2* cff = nullptr;
     unsigned long long k = 0;
     int depth = 0, nleaf = 0;
     double cum = 0.0, tol_unit = 0.0;
@@ -136,10 +139,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                     if (CODE < 0) code = curve_code(b, c);
                     const int64_t ci = b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
                     if constexpr (PREC == 1) {
-                        if constexpr (CODE >= 0)
-                            EvalFF<(CODE >= 0 ? CODE : 0)>::load(P.coef_ff + ci, rf);
-                        else
-                            load_ff_dyn(code, P.coef_ff + ci, rf);
+                        cff = P.coef_ff + ci;
                     } else {
                         if constexpr (CODE >= 0)
                             Eval<(CODE >= 0 ? CODE : 0)>::load_speed(t.coef + ci, r);
@@ -158,10 +158,13 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                         if (P.starts) {
                             const uint32_t q = P.starts[s];
                             float ch;
-                            if constexpr (PREC == 1)
-                                ch = chord_of<CODE>(rf);
-                            else
+                            if constexpr (PREC == 1) {
+                                ff rc[MAX_COEF];
+                                EvalFF<(CODE > 0 ? CODE : 16 + 4 + 2)>::load(cff, rc);
+                                ch = chord_of<CODE>(rc);
+                            } else {
                                 ch = chord_of<CODE>(r);
+                            }
                             if (q != 0u && ch > 0.0f) {
                                 dq = q;
                                 tol_unit = P.rtol * (double)ch;
@@ -209,10 +212,14 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
             ff Kf{0.0f, 0.0f};
             if constexpr (PREC == 1) {
                 ff Gf;
-                if constexpr (CODE >= 0)
-                    panel_k15_ff<(CODE >= 0 ? CODE : 0)>(rf, k, depth, Kf, Gf);
-                else
-                    panel_ff_dyn(code, rf, k, depth, Kf, Gf);
+                ff rl[MAX_COEF];
+                if constexpr (CODE >= 0) {
+                    EvalFF<(CODE >= 0 ? CODE : 0)>::load(cff, rl);
+                    panel_ff<(CODE >= 0 ? CODE : 0)>(rl, k, depth, Kf, Gf);
+                } else {
+                    load_ff_dyn(code, cff, rl);
+                    panel_ff_dyn(code, rl, k, depth, Kf, Gf);
+                }
                 if (depth == 0) {
                     tol_unit = P.rtol * fabs(ff_to_double(Kf));
                     tol_f = (float)tol_unit;
@@ -254,7 +261,12 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                     // shape the sampler's guess), -1 + (k + 1) 2^(1 - depth)
                     const float vr32 = fmaf((float)(k + 1), __int_as_float((128 - depth) << 23), -1.0f);
                     float q32;
-                    fend = (double)speed_slope32_of<CODE>(code, rf, vr32, q32);
+                    ff rl[MAX_COEF];
+                    if constexpr (CODE >= 0)
+                        EvalFF<(CODE >= 0 ? CODE : 0)>::load(cff, rl);
+                    else
+                        load_ff_dyn(code, cff, rl);
+                    fend = (double)speed_slope32_of<CODE>(code, rl, vr32, q32);
                     qend = (double)q32;
                 } else {
                     cum += K;
