@@ -1139,7 +1139,7 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, 
     P.n_samples = total;
     P.collect = c->opt.collect_stats;
     P.rtol = c->opt.rtol;
-    P.eps_frac = (float)(0.01 * c->opt.rtol);
+    P.eps_frac = (float)(SAMPLE_EPS_FRAC * c->opt.rtol);
     P.curve_list = nullptr;
     P.list_off = nullptr;
     P.cb = P.ce = 0;
@@ -1340,7 +1340,7 @@ gcv_status enqueue_sampling_graph(gcv_ctx* c, const int* d_counts, const double*
     P.out = d_out;
     P.collect = c->opt.collect_stats;
     P.rtol = c->opt.rtol;
-    P.eps_frac = (float)(0.01 * c->opt.rtol);
+    P.eps_frac = (float)(SAMPLE_EPS_FRAC * c->opt.rtol);
     // grids for any sample count: the kernels loop over their ranges
     const int64_t nominal = (int64_t)sm_count() * c->knobs.sample_blocks_per_sm * c->knobs.sample_threads;
     if (c->code >= 0) {

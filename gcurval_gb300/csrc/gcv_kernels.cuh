@@ -93,8 +93,8 @@ struct SampleParams {
     double* out;
     int64_t n_samples;
     int collect;
-    double rtol;  // the table's tolerance: samples are placed to 1 % of rtol * L
-    float eps_frac;  // 0.01 * rtol (the mixed sampler's stopping threshold over L)
+    double rtol;  // the table's tolerance: samples are placed to SAMPLE_EPS_FRAC of rtol * L
+    float eps_frac;  // SAMPLE_EPS_FRAC * rtol (the mixed sampler's stopping threshold over L)
     // Batches that mix curve codes run one launch per code over the curves
     // curve_list[cb .. ce) (grouped by code); list_off is the prefix of their
     // sample counts in that order.  curve_list NULL: all samples, curve order.
@@ -155,6 +155,12 @@ __device__ __forceinline__ int sample_curve_hint(const SampleParams& P, int64_t 
 }
 // samples per warp and turn in the mixed sampler (8 per lane, 32 apart)
 constexpr int SAMPLE_RUN = 256;
+
+// Newton stops once the estimated residual of its last step is below
+// SAMPLE_EPS_FRAC * rtol * L.  The table itself is good to rtol * L (the
+// length walk's per-interval tolerance, summed), so a tenth of that keeps a
+// sample's total error within 1.1 rtol * L.
+constexpr double SAMPLE_EPS_FRAC = 0.1;
 
 constexpr int SAMPLE_THREADS = 256;      // default block size
 constexpr int SAMPLE_THREADS_MAX = 512;  // largest block size the autotuner tries
@@ -323,9 +329,9 @@ __global__ void __launch_bounds__(SAMPLE_THREADS_MAX) k_sample(SampleParams P)
                     vg = fmin(fmax(vg, va), vb);
                 }
                 const double* seg = t.coef + b.coef_off[c] + (s - s0) * code_stride(code);
-                // stop when the residual of the last step is below 1 % of the
-                // sample tolerance rtol * L
-                const double eps_s = 0.01 * P.rtol * L;
+                // stop when the residual of the last step is below
+                // SAMPLE_EPS_FRAC * rtol * L
+                const double eps_s = SAMPLE_EPS_FRAC * P.rtol * L;
                 if constexpr (CODE >= 0) {
                     v = leaf_newton<(CODE >= 0 ? CODE : 0)>(seg, va, vb, base, cb, rr, vg, eps_s, newton);
                 } else {

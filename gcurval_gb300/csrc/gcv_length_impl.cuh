@@ -88,8 +88,12 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
 {
     __shared__ double lf_v[MODE == 0 ? LCAP : 1][LK_THREADS];
     __shared__ double lf_c[MODE == 0 ? LCAP : 1][LK_THREADS];
-    __shared__ float lf_f[MODE == 0 ? LCAP : 1][LK_THREADS];
-    __shared__ float lf_q[MODE == 0 ? LCAP : 1][LK_THREADS];
+    // the float-float path does not stage the leaves' end speed and slope:
+    // it re-evaluates them in FP32 when it flushes the leaves (same values),
+    // which leaves 16 of the 24 bytes per staged leaf and more blocks per SM
+    constexpr int FQ_ROWS = MODE == 0 && PREC == 0 ? LCAP : 1;
+    __shared__ float lf_f[FQ_ROWS][LK_THREADS];
+    __shared__ float lf_q[FQ_ROWS][LK_THREADS];
 
     const Batch& b = P.b;
     const Table& t = P.t;
@@ -184,8 +188,10 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                         if (MODE == 0) {
                             lf_v[0][tid] = 1.0;
                             lf_c[0][tid] = 0.0;
-                            lf_f[0][tid] = 0.0f;
-                            lf_q[0][tid] = 0.0f;
+                            if constexpr (PREC == 0) {
+                                lf_f[0][tid] = 0.0f;
+                                lf_q[0][tid] = 0.0f;
+                            }
                         } else if (MODE == 2 && pool >= 0) {
                             t.leaf_v[pool] = 1.0;
                             t.leaf_cum[pool] = 0.0;
@@ -257,17 +263,19 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                 if constexpr (PREC == 1) {
                     cumf = ff_add(cumf, Kf);
                     cum = ff_to_double(cumf);
-                    // the leaf's right-end speed and slope (FP32: they only
-                    // shape the sampler's guess), -1 + (k + 1) 2^(1 - depth)
-                    const float vr32 = fmaf((float)(k + 1), __int_as_float((128 - depth) << 23), -1.0f);
-                    float q32;
-                    ff rl[MAX_COEF];
-                    if constexpr (CODE >= 0)
-                        EvalFF<(CODE >= 0 ? CODE : 0)>::load(cff, rl);
-                    else
-                        load_ff_dyn(code, cff, rl);
-                    fend = (double)speed_slope32_of<CODE>(code, rl, vr32, q32);
-                    qend = (double)q32;
+                    if constexpr (MODE == 2) {
+                        // the leaf's right-end speed and slope (FP32: they only
+                        // shape the sampler's guess), -1 + (k + 1) 2^(1 - depth)
+                        const float vr32 = fmaf((float)(k + 1), __int_as_float((128 - depth) << 23), -1.0f);
+                        float q32;
+                        ff rl[MAX_COEF];
+                        if constexpr (CODE >= 0)
+                            EvalFF<(CODE >= 0 ? CODE : 0)>::load(cff, rl);
+                        else
+                            load_ff_dyn(code, cff, rl);
+                        fend = (double)speed_slope32_of<CODE>(code, rl, vr32, q32);
+                        qend = (double)q32;
+                    }
                 } else {
                     cum += K;
                 }
@@ -277,8 +285,10 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                     if (nleaf < LCAP) {
                         lf_v[nleaf][tid] = vr;
                         lf_c[nleaf][tid] = cum;
-                        lf_f[nleaf][tid] = (float)fend;
-                        lf_q[nleaf][tid] = (float)qend;
+                        if constexpr (PREC == 0) {
+                            lf_f[nleaf][tid] = (float)fend;
+                            lf_q[nleaf][tid] = (float)qend;
+                        }
                     } else {
                         ovf = true;
                     }
@@ -319,11 +329,28 @@ __global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
                 if (fin) {
                     const int64_t off = (int64_t)base + incl - x;
                     if (off + nleaf <= t.leaf_cap) {
-                        for (int i = 0; i < nleaf; ++i) {
-                            t.leaf_v[off + i] = lf_v[i][tid];
-                            t.leaf_cum[off + i] = lf_c[i][tid];
-                            t.leaf_f[off + i] = lf_f[i][tid];
-                            t.leaf_q[off + i] = lf_q[i][tid];
+                        if constexpr (PREC == 1) {
+                            ff rl[MAX_COEF];
+                            if constexpr (CODE >= 0)
+                                EvalFF<(CODE >= 0 ? CODE : 0)>::load(cff, rl);
+                            else
+                                load_ff_dyn(code, cff, rl);
+                            for (int i = 0; i < nleaf; ++i) {
+                                const double vi = lf_v[i][tid];
+                                float q32;
+                                const float f32 = speed_slope32_of<CODE>(code, rl, (float)vi, q32);
+                                t.leaf_v[off + i] = vi;
+                                t.leaf_cum[off + i] = lf_c[i][tid];
+                                t.leaf_f[off + i] = f32;
+                                t.leaf_q[off + i] = q32;
+                            }
+                        } else {
+                            for (int i = 0; i < nleaf; ++i) {
+                                t.leaf_v[off + i] = lf_v[i][tid];
+                                t.leaf_cum[off + i] = lf_c[i][tid];
+                                t.leaf_f[off + i] = lf_f[i][tid];
+                                t.leaf_q[off + i] = lf_q[i][tid];
+                            }
                         }
                     } else {
                         // the pool is full: the deep passes redo this interval
