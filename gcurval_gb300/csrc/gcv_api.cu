@@ -301,7 +301,6 @@ struct TuneKey {
 static std::mutex g_tune_m;
 static std::map<TuneKey, Knobs> g_tuned;
 
-constexpr int64_t LEARNED_CHUNK = 1 << 24;  // intervals per feature chunk of the learned form (1 GiB)
 constexpr int STREAM_EVENTS = 4;  // host-buffer sampling: events per stage, used round robin
 
 struct CodeRange {
@@ -335,7 +334,7 @@ struct gcv_ctx {
     // learned form: the network's weight image and per-interval start depths
     void* mlp_w = nullptr;
     DBuf<uint32_t> starts;
-    DBuf<float> feat;  // features of one chunk of intervals
+    DBuf<uint4> feat16;  // bf16 feature rows of the B-spline intervals (2 uint4 each), written by set-up
 
     // table
     DBuf<double> coef, seg_t0, seg_t1, seg_f0, seg_q0, seg_len, seg_cum, curve_len;
@@ -467,7 +466,7 @@ void destroy_ctx(gcv_ctx* c)
     c->seg_list.recycle();
     c->curve_list.recycle();
     c->starts.recycle();
-    c->feat.recycle();
+    c->feat16.recycle();
     if (c->mlp_w) cudaFree(c->mlp_w);
     c->list_sample_off.recycle();
     c->coef.recycle();
@@ -899,7 +898,8 @@ gcv_status tune_after_sampling(gcv_ctx* c)
     return GCV_OK;
 }
 
-gcv_status launch_setup_list(gcv_ctx* c, const CodeRange& r)
+// feat16: the learned form's feature rows in grouped-list order (NULL otherwise)
+gcv_status launch_setup_list(gcv_ctx* c, const CodeRange& r, uint4* feat16)
 {
     const int64_t n = r.end - r.begin;
     if (n <= 0) return GCV_OK;
@@ -907,9 +907,11 @@ gcv_status launch_setup_list(gcv_ctx* c, const CodeRange& r)
     const Batch b = batch_view(c);
     const Table t = table_view(c);
     const int* list = c->seg_list.p + r.begin;
+    uint4* f16 = feat16 && r.code != CODE_ELLIPSE ? feat16 + 2 * r.begin : nullptr;
+    const float rf = rtol_feature(c->opt.rtol);
     switch (r.code) {
 #define GCV_CASE(C)                                                                                \
-    case C: k_setup_list<C><<<blocks, 256, 0, c->stream>>>(b, t, list, n); break;
+    case C: k_setup_list<C><<<blocks, 256, 0, c->stream>>>(b, t, list, n, f16, rf); break;
         GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
     default: return fail(GCV_ERR_INVALID, "no set-up kernel for curve code " + std::to_string(r.code));
@@ -926,36 +928,38 @@ gcv_status build_table(gcv_ctx* c)
     const bool mixed = c->opt.precision == GCV_MIXED;
     const Batch b = batch_view(c);
     const int setup_blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 64));
+    const bool learned = c->opt.learned && c->mlp_w && c->n_seg > 0;
+    // the learned form's set-up also writes each B-spline interval's features
+    const bool with_features = learned && c->code != CODE_ELLIPSE;
+    if (with_features) CHECK(c->feat16.reserve((size_t)c->n_seg * 2));
+    uint4* feat16 = with_features ? c->feat16.p : nullptr;
     CU(cudaEventRecord(c->ev[0], c->stream));
     CU(cudaMemsetAsync(c->ctr.p, 0, C_COUNT * sizeof(unsigned long long), c->stream));
     if (c->n_seg > 0 && c->code >= 0) {
-        k_setup<<<setup_blocks, 256, 0, c->stream>>>(b, table_view(c));
+        k_setup<<<setup_blocks, 256, 0, c->stream>>>(b, table_view(c), feat16, rtol_feature(c->opt.rtol));
         CU(cudaGetLastError());
         c->stats.n_launches++;
     } else if (c->n_seg > 0) {
-        for (const CodeRange& r : c->code_ranges) CHECK(launch_setup_list(c, r));
+        for (const CodeRange& r : c->code_ranges) CHECK(launch_setup_list(c, r, feat16));
     }
     CU(cudaEventRecord(c->ev[1], c->stream));
-    const bool learned = c->opt.learned && c->mlp_w && c->n_seg > 0;
     if (learned) {
         // start depths of every B-spline interval from the network (ellipse pieces keep 0)
         CHECK(c->starts.reserve((size_t)c->n_seg));
         CU(cudaMemsetAsync(c->starts.p, 0, (size_t)c->n_seg * sizeof(uint32_t), c->stream));
         const int md = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
-        const int64_t rows = std::min<int64_t>(c->n_seg, LEARNED_CHUNK);
-        CHECK(c->feat.reserve((size_t)rows * MLP_IN));
-        auto run = [&](const int* list, int64_t n) -> gcv_status {
-            cudaError_t e = mlp_starts_launch(b, list, n, c->mlp_w, c->opt.rtol, md, c->starts.p, c->feat.p, rows,
-                                              c->stream);
+        auto run = [&](const uint4* f16, const int* list, int64_t n) -> gcv_status {
+            cudaError_t e = mlp_starts_launch_bf16(f16, list, n, c->mlp_w, md, c->starts.p, c->stream);
             if (e != cudaSuccess) return cuda_fail(e, "network inference");
             c->stats.n_launches++;
             return GCV_OK;
         };
         if (c->code > 0) {
-            CHECK(run(nullptr, c->n_seg));
+            CHECK(run(c->feat16.p, nullptr, c->n_seg));
         } else if (c->code < 0) {
             for (const CodeRange& r : c->code_ranges)
-                if (r.code != CODE_ELLIPSE) CHECK(run(c->seg_list.p + r.begin, r.end - r.begin));
+                if (r.code != CODE_ELLIPSE)
+                    CHECK(run(c->feat16.p + 2 * r.begin, c->seg_list.p + r.begin, r.end - r.begin));
         }
     }
     CU(cudaEventRecord(c->ev[6], c->stream));
@@ -1239,32 +1243,33 @@ gcv_status enqueue_table_graph(gcv_ctx* c)
 {
     const bool mixed = c->opt.precision == GCV_MIXED;
     const Batch b = batch_view(c);
+    const bool learned = c->opt.learned && c->mlp_w && c->n_seg > 0;
+    // feat16 is reserved before the capture (gcv_step_graph)
+    uint4* feat16 = learned && c->code != CODE_ELLIPSE ? c->feat16.p : nullptr;
     CU(cudaEventRecordWithFlags(c->ev[0], c->stream, cudaEventRecordExternal));
     CU(cudaMemsetAsync(c->ctr.p, 0, C_COUNT * sizeof(unsigned long long), c->stream));
     if (c->n_seg > 0 && c->code >= 0) {
         const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((c->n_seg + 255) / 256, (int64_t)sm_count() * 64));
-        k_setup<<<blocks, 256, 0, c->stream>>>(b, table_view(c));
+        k_setup<<<blocks, 256, 0, c->stream>>>(b, table_view(c), feat16, rtol_feature(c->opt.rtol));
         CU(cudaGetLastError());
     } else if (c->n_seg > 0) {
-        for (const CodeRange& r : c->code_ranges) CHECK(launch_setup_list(c, r));
+        for (const CodeRange& r : c->code_ranges) CHECK(launch_setup_list(c, r, feat16));
     }
     CU(cudaEventRecordWithFlags(c->ev[1], c->stream, cudaEventRecordExternal));
-    const bool learned = c->opt.learned && c->mlp_w && c->n_seg > 0;
     if (learned) {
         CU(cudaMemsetAsync(c->starts.p, 0, (size_t)c->n_seg * sizeof(uint32_t), c->stream));
         const int md = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
-        const int64_t rows = std::min<int64_t>(c->n_seg, LEARNED_CHUNK);
-        auto run = [&](const int* list, int64_t n) -> gcv_status {
-            cudaError_t e = mlp_starts_launch(b, list, n, c->mlp_w, c->opt.rtol, md, c->starts.p, c->feat.p, rows,
-                                              c->stream);
+        auto run = [&](const uint4* f16, const int* list, int64_t n) -> gcv_status {
+            cudaError_t e = mlp_starts_launch_bf16(f16, list, n, c->mlp_w, md, c->starts.p, c->stream);
             if (e != cudaSuccess) return cuda_fail(e, "network inference");
             return GCV_OK;
         };
         if (c->code > 0) {
-            CHECK(run(nullptr, c->n_seg));
+            CHECK(run(c->feat16.p, nullptr, c->n_seg));
         } else if (c->code < 0) {
             for (const CodeRange& r : c->code_ranges)
-                if (r.code != CODE_ELLIPSE) CHECK(run(c->seg_list.p + r.begin, r.end - r.begin));
+                if (r.code != CODE_ELLIPSE)
+                    CHECK(run(c->feat16.p + 2 * r.begin, c->seg_list.p + r.begin, r.end - r.begin));
         }
     }
     CU(cudaEventRecordWithFlags(c->ev[6], c->stream, cudaEventRecordExternal));
@@ -2050,7 +2055,7 @@ gcv_status gcv_step_graph(gcv_ctx* ctx, const int* d_counts, const double* d_pos
         CHECK(c->scan_blk.reserve((size_t)(c->n_curve + 1023) / 1024 + 1));
         if (c->opt.learned && c->mlp_w) {
             CHECK(c->starts.reserve((size_t)std::max<int64_t>(c->n_seg, 1)));
-            CHECK(c->feat.reserve((size_t)std::min<int64_t>(std::max<int64_t>(c->n_seg, 1), LEARNED_CHUNK) * MLP_IN));
+            if (c->code != CODE_ELLIPSE) CHECK(c->feat16.reserve((size_t)std::max<int64_t>(c->n_seg, 1) * 2));
         }
         if (!c->stream && !c->gstream) CU(cudaStreamCreateWithFlags(&c->gstream, cudaStreamNonBlocking));
         cudaStream_t user = c->stream;

@@ -119,6 +119,26 @@ __device__ inline void interval_features(const Batch& b, int64_t s, float log_rt
 // feature 15: -log10(rtol) / 10
 inline float rtol_feature(double rtol) { return (float)(-std::log10(rtol) * 0.1); }
 
+// The features of interval s as one bf16 row (16 values, 32 bytes, rounded
+// to nearest: the same bf16 values the network kernel would make of the FP32
+// row), written by the set-up kernels of the learned form so that no separate
+// pass gathers the knots and control points again.
+__device__ __forceinline__ void write_feature_row_bf16(const Batch& b, int64_t s, float log_rtol_feature,
+                                                       uint4* __restrict__ row)
+{
+    float f[MLP_IN];
+    interval_features(b, s, log_rtol_feature, f);
+    uint32_t w[MLP_IN / 2];
+#pragma unroll
+    for (int i = 0; i < MLP_IN / 2; ++i) {
+        uint32_t h;
+        asm("cvt.rn.bf16x2.f32 %0, %2, %1;" : "=r"(h) : "f"(f[2 * i]), "f"(f[2 * i + 1]));
+        w[i] = h;
+    }
+    row[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    row[1] = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
 // Start depth of the learned walk for the node (k, depth): the quarter
 // depths dq (one byte each) of the quarters the node covers (their minimum
 // above depth 2).
@@ -169,12 +189,11 @@ __device__ __forceinline__ uint32_t quarter_depths(const float* o, int max_depth
     return out;
 }
 
-// Start depths of the intervals list[0 .. n) (list NULL: 0 .. n - 1) into
-// starts[s]: in chunks of feat_rows intervals, their features into `feat`
-// (feat_rows x 16 floats), then the tcgen05 network over the chunk (defined
-// in gcv_mlp_tc.cu).  w_dev: the device copy made by mlp_upload_bf16.
-cudaError_t mlp_starts_launch(const Batch& b, const int* list, int64_t n, const void* w_dev, double rtol,
-                              int max_depth, uint32_t* starts, float* feat, int64_t feat_rows, cudaStream_t stream);
+// Start depths of the intervals list[0 .. n) (list NULL: 0 .. n - 1) from
+// their bf16 feature rows feat16[0 .. n) (two uint4 each, written by the
+// set-up kernels): one launch of the tcgen05 network.
+cudaError_t mlp_starts_launch_bf16(const uint4* feat16, const int* list, int64_t n, const void* w_dev, int max_depth,
+                                   uint32_t* starts, cudaStream_t stream);
 // device copy of the packed FP32 weights in the inference kernel's layout
 cudaError_t mlp_upload_bf16(const float* host_w, void** w_dev);
 size_t mlp_dev_bytes();

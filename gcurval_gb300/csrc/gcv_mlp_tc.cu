@@ -2,7 +2,8 @@
 //
 // One CTA = four warpgroups; each warpgroup runs its own tiles of 128
 // intervals (M = 128 rows, one row per thread and TMEM lane):
-//   features (FP32 rows, written by k_feature_rows) -> bf16 tile X [128 x 16]
+//   features (bf16 rows written by the set-up kernels, or FP32 rows for the
+//   raw-output entry point) -> bf16 tile X [128 x 16]
 //   D = X W1        1 x tcgen05.mma (K = 16), D in TMEM (128 lanes x 128 cols, FP32)
 //   H1 = 2 GELU(D + b1) -> bf16 tile [128 x 128] in shared memory (the
 //        factor 2 is taken back by W2, W3, W4 stored halved: exact in bf16)
@@ -171,7 +172,8 @@ __device__ __forceinline__ void st_bf16x8(uint8_t* p, const float* v)
 }
 
 struct TcArgs {
-    const float* feat;  // n rows of MLP_IN features
+    const float* feat;  // n rows of MLP_IN features (FP32), or
+    const uint4* feat16;  // n rows of MLP_IN bf16 features (two uint4 per row)
     int64_t n;
     // product path: start depths of intervals list[row0 + row] (list NULL: row0 + row)
     const int* list;
@@ -184,8 +186,9 @@ struct TcArgs {
     unsigned* err;
 };
 
-// STARTS: start depths out; else the raw outputs
-template <bool STARTS>
+// STARTS: start depths out; else the raw outputs.  BF16IN: the rows come as
+// bf16 (feat16) and go to the operand tile as they are.
+template <bool STARTS, bool BF16IN>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
 {
     extern __shared__ __align__(1024) uint8_t sm[];
@@ -223,12 +226,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
     bool ok = true;
 
     const int64_t tiles = (A.n + 127) / 128;
-    float4 nxt[MLP_IN / 4];
+    float4 nxt[BF16IN ? 1 : MLP_IN / 4];
+    uint4 nxt16[2];
     auto load_rows = [&](int64_t tl) {
         const int64_t r = tl * 128 + t;
-        const float4* src = reinterpret_cast<const float4*>(A.feat + r * MLP_IN);
+        if constexpr (BF16IN) {
+            nxt16[0] = r < A.n ? A.feat16[2 * r] : make_uint4(0u, 0u, 0u, 0u);
+            nxt16[1] = r < A.n ? A.feat16[2 * r + 1] : make_uint4(0u, 0u, 0u, 0u);
+        } else {
+            const float4* src = reinterpret_cast<const float4*>(A.feat + r * MLP_IN);
 #pragma unroll
-        for (int i = 0; i < MLP_IN / 4; ++i) nxt[i] = r < A.n ? src[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            for (int i = 0; i < MLP_IN / 4; ++i) nxt[i] = r < A.n ? src[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
     };
     load_rows((int64_t)blockIdx.x * NWG + wg);
     for (int64_t tile = (int64_t)blockIdx.x * NWG + wg; tile < tiles && ok; tile += (int64_t)gridDim.x * NWG) {
@@ -236,17 +245,24 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
         const bool live = row < A.n;
         // ---- features -> X (bf16, K-major core matrices, K = 16); the next
         // tile's rows are fetched now and used one iteration later
-        float f[MLP_IN];
+        if constexpr (BF16IN) {
+            const uint4 x0 = nxt16[0], x1 = nxt16[1];
+            load_rows(tile + (int64_t)gridDim.x * NWG);
+            *reinterpret_cast<uint4*>(X + kmaj_off(t, 0, MLP_IN)) = x0;
+            *reinterpret_cast<uint4*>(X + kmaj_off(t, 8, MLP_IN)) = x1;
+        } else {
+            float f[MLP_IN];
 #pragma unroll
-        for (int i = 0; i < MLP_IN / 4; ++i) {
-            f[4 * i] = nxt[i].x;
-            f[4 * i + 1] = nxt[i].y;
-            f[4 * i + 2] = nxt[i].z;
-            f[4 * i + 3] = nxt[i].w;
+            for (int i = 0; i < MLP_IN / 4; ++i) {
+                f[4 * i] = nxt[i].x;
+                f[4 * i + 1] = nxt[i].y;
+                f[4 * i + 2] = nxt[i].z;
+                f[4 * i + 3] = nxt[i].w;
+            }
+            load_rows(tile + (int64_t)gridDim.x * NWG);
+            st_bf16x8(X + kmaj_off(t, 0, MLP_IN), f);
+            st_bf16x8(X + kmaj_off(t, 8, MLP_IN), f + 8);
         }
-        load_rows(tile + (int64_t)gridDim.x * NWG);
-        st_bf16x8(X + kmaj_off(t, 0, MLP_IN), f);
-        st_bf16x8(X + kmaj_off(t, 8, MLP_IN), f + 8);
         fence_async_smem();
         fence_before();
         wg_sync(wg);
@@ -340,27 +356,14 @@ int sm_count_tc()
     return n;
 }
 
-// features of intervals list[row0 + r] (list NULL: row0 + r) as FP32 rows
-__global__ void k_feature_rows(Batch b, const int* list, int64_t row0, int64_t n, float rtol_feat, float* out)
-{
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = list ? (int64_t)list[row0 + r] : row0 + r;
-        float f[MLP_IN];
-        interval_features(b, s, rtol_feat, f);
-        float4* dst = reinterpret_cast<float4*>(out + r * MLP_IN);
-#pragma unroll
-        for (int i = 0; i < MLP_IN / 4; ++i) dst[i] = make_float4(f[4 * i], f[4 * i + 1], f[4 * i + 2], f[4 * i + 3]);
-    }
-}
-
-template <bool STARTS>
+template <bool STARTS, bool BF16IN = false>
 cudaError_t launch_tc(const TcArgs& A, cudaStream_t stream)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc<STARTS>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES);
+    cudaError_t e = cudaFuncSetAttribute(k_mlp_tc<STARTS, BF16IN>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM_BYTES);
     if (e != cudaSuccess) return e;
     const int64_t tiles = (A.n + 127) / 128;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((tiles + NWG - 1) / NWG, sm_count_tc()));
-    k_mlp_tc<STARTS><<<grid, TC_THREADS, SM_BYTES, stream>>>(A);
+    k_mlp_tc<STARTS, BF16IN><<<grid, TC_THREADS, SM_BYTES, stream>>>(A);
     return cudaGetLastError();
 }
 
@@ -406,29 +409,20 @@ cudaError_t mlp_upload_bf16(const float* host_w, void** w_dev)
     return e;
 }
 
-cudaError_t mlp_starts_launch(const Batch& b, const int* list, int64_t n, const void* w_dev, double rtol, int max_depth,
-                              uint32_t* starts, float* feat, int64_t feat_rows, cudaStream_t stream)
+cudaError_t mlp_starts_launch_bf16(const uint4* feat16, const int* list, int64_t n, const void* w_dev, int max_depth,
+                                   uint32_t* starts, cudaStream_t stream)
 {
-    const float rf = rtol_feature(rtol);
-    for (int64_t o = 0; o < n; o += feat_rows) {
-        const int64_t m = std::min<int64_t>(feat_rows, n - o);
-        const int blocks = (int)std::min<int64_t>((m + 255) / 256, (int64_t)sm_count_tc() * 32);
-        k_feature_rows<<<blocks, 256, 0, stream>>>(b, list, o, m, rf, feat);
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        TcArgs A{};
-        A.feat = feat;
-        A.n = m;
-        A.list = list;
-        A.row0 = o;
-        A.max_depth = max_depth;
-        A.starts = starts;
-        A.w = (const uint8_t*)w_dev;
-        A.err = (unsigned*)((uint8_t*)w_dev + WB_BYTES);
-        e = launch_tc<true>(A, stream);
-        if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    if (n <= 0) return cudaSuccess;
+    TcArgs A{};
+    A.feat16 = feat16;
+    A.n = n;
+    A.list = list;
+    A.row0 = 0;
+    A.max_depth = max_depth;
+    A.starts = starts;
+    A.w = (const uint8_t*)w_dev;
+    A.err = (unsigned*)((uint8_t*)w_dev + WB_BYTES);
+    return launch_tc<true, true>(A, stream);
 }
 
 }  // namespace gcv

@@ -51,11 +51,14 @@ __device__ __forceinline__ void setup_bspline_any(const Batch& b, const Table& t
         setup_bspline_seg<P, D>(b, t, s, c);
 }
 
-static __global__ void k_setup(Batch b, Table t)
+// feat16 (learned form only, else NULL): bf16 feature row of every B-spline
+// segment s at feat16[2 s]
+static __global__ void k_setup(Batch b, Table t, uint4* __restrict__ feat16, float rtol_feat)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < b.n_seg;
          s += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = b.seg_curve[s];
+        if (feat16 && b.kind[c] != 0) write_feature_row_bf16(b, s, rtol_feat, feat16 + 2 * s);
         switch (curve_code(b, c)) {
         case CODE_ELLIPSE: setup_ellipse_seg(b, t, s, c); break;
 #define GCV_SETUP_CASE(P, D)                                                                       \
@@ -69,17 +72,22 @@ static __global__ void k_setup(Batch b, Table t)
     }
 }
 
-// set-up of the segments list[0 .. n) of one curve code (batches that mix codes)
+// set-up of the segments list[0 .. n) of one curve code (batches that mix
+// codes); feat16 (learned form, B-spline codes; else NULL): the bf16 feature
+// row of list[i] at feat16[2 i]
 template <int CODE>
-__global__ void k_setup_list(Batch b, Table t, const int* __restrict__ list, int64_t n)
+__global__ void k_setup_list(Batch b, Table t, const int* __restrict__ list, int64_t n, uint4* __restrict__ feat16,
+                             float rtol_feat)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t s = list[i];
         const int64_t c = b.seg_curve[s];
-        if constexpr (CODE == CODE_ELLIPSE)
+        if constexpr (CODE == CODE_ELLIPSE) {
             setup_ellipse_seg(b, t, s, c);
-        else
+        } else {
+            if (feat16) write_feature_row_bf16(b, s, rtol_feat, feat16 + 2 * i);
             setup_bspline_any<code_degree(CODE), code_dim(CODE)>(b, t, s, c);
+        }
     }
 }
 
