@@ -116,6 +116,65 @@ __device__ inline void interval_features(const Batch& b, int64_t s, float log_rt
     f[13] = wr > 0.0f ? fminf(fmaxf(__log2f(wr / w), -8.0f), 8.0f) * 0.125f : -1.0f;
 }
 
+// interval_features for a B-spline interval of compile-time degree P and
+// dimension D (the per-code set-up kernels): the same operations in the same
+// order, with the loops unrolled and the polygon held in registers.
+template <int P, int D>
+__device__ __forceinline__ void interval_features_pd(const Batch& b, int64_t s, float log_rtol_feature, float* f)
+{
+#pragma unroll
+    for (int i = 0; i < MLP_IN; ++i) f[i] = 0.0f;
+    const int64_t c = b.seg_curve[s];
+    const int64_t j = s - b.seg_off[c];
+    const double* kv = b.knots + b.knot_off[c];
+    const double* cp = b.ctrl + b.ctrl_off[c];
+    const int span = int(j) + P;
+    const double k0 = kv[span];
+    const float fk0 = float_of(k0);
+    const float w = float_of(kv[span + 1]) - fk0;
+    f[0] = P * 0.2f;
+    f[1] = (float)(D - 2);
+    f[15] = log_rtol_feature;
+    if (!(w > 0.0f)) return;
+    float q[P + 1][3], base[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) base[d] = d < D ? float_of(cp[(size_t)(span - P) * D + d]) : 0.0f;
+#pragma unroll
+    for (int i = 0; i <= P; ++i)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) q[i][d] = d < D ? float_of(cp[(size_t)(span - P + i) * D + d]) - base[d] : 0.0f;
+    float e[P], sum = 0.0f;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+        const float dx = q[i + 1][0] - q[i][0], dy = q[i + 1][1] - q[i][1], dz = q[i + 1][2] - q[i][2];
+        e[i] = sqrtf(dx * dx + dy * dy + dz * dz);
+        sum += e[i];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) f[7 + i] = 1.0f;
+    if (sum > 0.0f) {
+        const float inv = 1.0f / sum;
+#pragma unroll
+        for (int i = 0; i < P; ++i) f[2 + i] = e[i] * inv;
+#pragma unroll
+        for (int i = 0; i + 1 < P; ++i) {
+            float dot = 0.0f;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) dot += (q[i + 1][d] - q[i][d]) * (q[i + 2][d] - q[i + 1][d]);
+            const float den = e[i] * e[i + 1];
+            f[7 + i] = den > 0.0f ? fminf(fmaxf(dot / den, -1.0f), 1.0f) : 1.0f;
+        }
+        const float cx = q[P][0], cy = q[P][1], cz = q[P][2];
+        const float chord = sqrtf(cx * cx + cy * cy + cz * cz);
+        f[14] = chord > 0.0f ? fminf(fmaxf(__log2f(sum / chord), 0.0f), 8.0f) * 0.25f : 2.0f;
+    }
+    const float support = float_of(kv[span + P + 1]) - float_of(kv[span - P]);
+    f[11] = support > 0.0f ? w / support : 0.0f;
+    const float wl = fk0 - float_of(kv[span - 1]), wr = float_of(kv[span + 2]) - float_of(kv[span + 1]);
+    f[12] = wl > 0.0f ? fminf(fmaxf(__log2f(wl / w), -8.0f), 8.0f) * 0.125f : -1.0f;
+    f[13] = wr > 0.0f ? fminf(fmaxf(__log2f(wr / w), -8.0f), 8.0f) * 0.125f : -1.0f;
+}
+
 // feature 15: -log10(rtol) / 10
 inline float rtol_feature(double rtol) { return (float)(-std::log10(rtol) * 0.1); }
 
@@ -123,11 +182,17 @@ inline float rtol_feature(double rtol) { return (float)(-std::log10(rtol) * 0.1)
 // to nearest: the same bf16 values the network kernel would make of the FP32
 // row), written by the set-up kernels of the learned form so that no separate
 // pass gathers the knots and control points again.
+// P > 0: the interval's curve has compile-time degree P and dimension D;
+// P == 0: read them from the batch
+template <int P = 0, int D = 0>
 __device__ __forceinline__ void write_feature_row_bf16(const Batch& b, int64_t s, float log_rtol_feature,
                                                        uint4* __restrict__ row)
 {
     float f[MLP_IN];
-    interval_features(b, s, log_rtol_feature, f);
+    if constexpr (P > 0)
+        interval_features_pd<P, D>(b, s, log_rtol_feature, f);
+    else
+        interval_features(b, s, log_rtol_feature, f);
     uint32_t w[MLP_IN / 2];
 #pragma unroll
     for (int i = 0; i < MLP_IN / 2; ++i) {

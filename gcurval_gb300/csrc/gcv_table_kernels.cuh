@@ -85,7 +85,8 @@ __global__ void k_setup_list(Batch b, Table t, const int* __restrict__ list, int
         if constexpr (CODE == CODE_ELLIPSE) {
             setup_ellipse_seg(b, t, s, c);
         } else {
-            if (feat16) write_feature_row_bf16(b, s, rtol_feat, feat16 + 2 * i);
+            if (feat16)
+                write_feature_row_bf16<code_degree(CODE), code_dim(CODE)>(b, s, rtol_feat, feat16 + 2 * i);
             setup_bspline_any<code_degree(CODE), code_dim(CODE)>(b, t, s, c);
         }
     }
