@@ -436,6 +436,12 @@ class Bench:
             r["leaves"] = st1["n_leaves"]
             r["deep"] = st1["n_deep_segments"]
             r["capped"] = st1["n_capped"]
+            slots = ["ellipse"] + [f"p{p}d{d}" for d in (2, 3) for p in range(1, 6)]
+            r["launch_shapes"] = {"tuned": bool(st1["tuned"]),
+                                  "length_workers_per_sm": {n: v for n, v in zip(slots, st1["length_blocks_per_sm_code"])},
+                                  "deep_workers_per_sm": st1["length_blocks_per_sm"],
+                                  "sample_threads": st1["sample_threads"],
+                                  "sample_blocks_per_sm": st1["sample_blocks_per_sm"]}
             r["ms_per_step"] = total_ms / steps
             r["steps"] = steps
             r["clocks"] = clk.summary() if clocks else None
@@ -695,6 +701,7 @@ def main():
                     "d2h_bytes_per_step": int(d2h), "samples_per_s": round(world * n_samples / e2e_s, 1),
                     "ms_per_step": round(e2e_s * 1e3, 3), "breakdown_ms": e2e_parts},
             "gpu_launches": int(main_r["launches"]),
+            "launch_shapes": main_r["launch_shapes"],
             "roofline": roofline,
             "cpu_baseline": cpu,
             "accuracy_vs_fp64_oracle": acc,

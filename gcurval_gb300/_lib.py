@@ -63,10 +63,13 @@ class Stats(ctypes.Structure):
                 ("ms_length", ctypes.c_double), ("ms_scan", ctypes.c_double), ("ms_sample", ctypes.c_double),
                 ("n_launches", ctypes.c_int64), ("ms_learned", ctypes.c_double),
                 ("length_blocks_per_sm", ctypes.c_int), ("sample_threads", ctypes.c_int),
-                ("sample_blocks_per_sm", ctypes.c_int), ("tuned", ctypes.c_int)]
+                ("sample_blocks_per_sm", ctypes.c_int), ("tuned", ctypes.c_int),
+                ("length_blocks_per_sm_code", ctypes.c_int * 11)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["length_blocks_per_sm_code"] = list(d["length_blocks_per_sm_code"])
+        return d
 
 
 _SIGS = {

@@ -259,33 +259,48 @@ int sm_count()
 
 }  // namespace
 
+// the curve codes' slots in per-code tables: ellipse 0, then degree 1-5 in
+// 2D (1-5) and in 3D (6-10)
+constexpr int N_CODE_SLOTS = GCV_N_CODE_SLOTS;
+inline int code_slot(int code) { return code == CODE_ELLIPSE ? 0 : 1 + (code_dim(code) - 2) * 5 + (code_degree(code) - 1); }
+
 // Launch shapes picked by the autotuner: persistent length workers per SM
-// (cap on the occupancy) and the sampling kernels' block size and blocks per SM.
+// (cap on the occupancy) for each curve code's main pass and for the deep
+// passes, and the sampling kernels' block size and blocks per SM.
 struct Knobs {
-    int length_cap = 32;
+    int length_cap[N_CODE_SLOTS];
+    int deep_cap = 32;
     int sample_threads = 256;
     int sample_blocks_per_sm = 64;
+    Knobs()
+    {
+        for (int& x : length_cap) x = 32;
+    }
     bool operator==(const Knobs& o) const
     {
-        return length_cap == o.length_cap && sample_threads == o.sample_threads &&
-               sample_blocks_per_sm == o.sample_blocks_per_sm;
+        return std::memcmp(length_cap, o.length_cap, sizeof(length_cap)) == 0 && deep_cap == o.deep_cap &&
+               sample_threads == o.sample_threads && sample_blocks_per_sm == o.sample_blocks_per_sm;
     }
 };
 // The first TUNE_TRIALS table builds (and samplings) of a batch shape not seen
-// before in the process each run one candidate; the fastest length and
-// sampling shapes, timed by the context's events, are kept for that shape
-// (curve code, precision, learned form, log2 of the interval count).  The
-// shapes change scheduling only: every result is the same under each.
+// before in the process each run one candidate; the fastest shapes, timed by
+// the context's events, are kept for that shape (curve code, precision,
+// learned form, log2 of the interval count).  The length walk is timed code
+// by code (its main pass launches once per curve code), so each code of a
+// batch that mixes codes keeps the persistent-worker count that was fastest
+// for it.  The shapes change scheduling only: every result is the same under
+// each.
 constexpr int TUNE_TRIALS = 3;
+inline int trial_length_cap(int i) { return i == 1 ? 4 : (i == 2 ? 6 : 32); }
 inline Knobs trial_knobs(int i)
 {
     Knobs k;
+    for (int& x : k.length_cap) x = trial_length_cap(i);
+    k.deep_cap = trial_length_cap(i);
     if (i == 1) {
-        k.length_cap = 4;
         k.sample_threads = 128;
         k.sample_blocks_per_sm = 128;
     } else if (i == 2) {
-        k.length_cap = 6;
         k.sample_threads = 512;
         k.sample_blocks_per_sm = 16;
     }
@@ -377,6 +392,11 @@ struct gcv_ctx {
     // autotuner progress of this context (-1: tuned, shapes from the table)
     int len_trial = 0, smp_trial = 0;
     double len_ms[TUNE_TRIALS] = {}, smp_ms[TUNE_TRIALS] = {};
+    // per-code main-pass times of the tuning builds (ev_code: start / end of
+    // each code's main-pass launch in the last build)
+    double len_code_ms[TUNE_TRIALS][N_CODE_SLOTS] = {};
+    cudaEvent_t ev_code[N_CODE_SLOTS][2] = {};
+    bool code_timed[N_CODE_SLOTS] = {};
     TuneKey tune_key{-9, -9, -9, -9};
     // chunked host <-> device streaming of samples
     cudaStream_t s_in = nullptr, s_out = nullptr;
@@ -509,6 +529,9 @@ void destroy_ctx(gcv_ctx* c)
     if (c->s_out) cudaStreamDestroy(c->s_out);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& pair : c->ev_code)
+        for (auto& e : pair)
+            if (e) cudaEventDestroy(e);
     delete c;
 }
 
@@ -585,6 +608,8 @@ gcv_status finish_create(gcv_ctx* c, const uint8_t* kind, const uint8_t* degree,
     CHECK(c->ctr.reserve(C_COUNT));
     CU(cudaMallocHost(&c->h_ctr, C_COUNT * sizeof(unsigned long long)));
     for (auto& e : c->ev) CU(cudaEventCreate(&e));
+    for (auto& pair : c->ev_code)
+        for (auto& e : pair) CU(cudaEventCreate(&e));
     if (c->n_curve > 0) {
         const Batch b = batch_view(c);
         const int blocks = (int)std::min<int64_t>((c->n_curve + 255) / 256, 65535);
@@ -768,19 +793,21 @@ gcv_status launch_length_code(gcv_ctx* c, int code, const LengthParams& P)
     const int sms = sm_count();
     cudaError_t e = cudaErrorInvalidValue;
     if constexpr (MODE == 0) {
+        const int cap = c->knobs.length_cap[code_slot(code)];
         switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: e = length_launch<0, C, PREC>(P, c->stream, sms, c->knobs.length_cap); break;
+    case C: e = length_launch<0, C, PREC>(P, c->stream, sms, cap); break;
             GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
         default: return fail(GCV_ERR_INVALID, "no length kernel for curve code " + std::to_string(code));
         }
     } else {
+        const int cap = c->knobs.deep_cap;
         switch (code) {
-        case CODE_ELLIPSE: e = length_launch<MODE, CODE_ELLIPSE, PREC>(P, c->stream, sms, c->knobs.length_cap); break;
-        case bs_code(3, 2): e = length_launch<MODE, bs_code(3, 2), PREC>(P, c->stream, sms, c->knobs.length_cap); break;
-        case bs_code(3, 3): e = length_launch<MODE, bs_code(3, 3), PREC>(P, c->stream, sms, c->knobs.length_cap); break;
-        default: e = length_launch<MODE, -1, PREC>(P, c->stream, sms, c->knobs.length_cap); break;
+        case CODE_ELLIPSE: e = length_launch<MODE, CODE_ELLIPSE, PREC>(P, c->stream, sms, cap); break;
+        case bs_code(3, 2): e = length_launch<MODE, bs_code(3, 2), PREC>(P, c->stream, sms, cap); break;
+        case bs_code(3, 3): e = length_launch<MODE, bs_code(3, 3), PREC>(P, c->stream, sms, cap); break;
+        default: e = length_launch<MODE, -1, PREC>(P, c->stream, sms, cap); break;
         }
     }
     if (e != cudaSuccess) return cuda_fail(e, "length kernel launch");
@@ -796,14 +823,25 @@ gcv_status launch_length(gcv_ctx* c, int code, const LengthParams& P)
 }
 
 // Main pass: one launch over all segments of a uniform batch, or one launch
-// per curve code over that code's range of the grouped segment list.
-gcv_status launch_main_pass(gcv_ctx* c, LengthParams P)
+// per curve code over that code's range of the grouped segment list; each
+// code's launch is bracketed by its pair of timing events (as external event
+// nodes under stream capture), which the autotuner reads.
+gcv_status launch_main_pass(gcv_ctx* c, LengthParams P, bool capture = false)
 {
+    auto mark = [&](int code, int which) -> gcv_status {
+        cudaEvent_t e = c->ev_code[code_slot(code)][which];
+        CU(capture ? cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal) : cudaEventRecord(e, c->stream));
+        c->code_timed[code_slot(code)] = true;
+        return GCV_OK;
+    };
+    for (bool& x : c->code_timed) x = false;
     if (c->code >= 0) {
         P.list = nullptr;
         P.n_items = c->n_seg;
         P.work = c->ctr.p + C_WORK;
-        return launch_length<0>(c, c->code, P);
+        CHECK(mark(c->code, 0));
+        CHECK(launch_length<0>(c, c->code, P));
+        return mark(c->code, 1);
     }
     for (size_t k = 0; k < c->code_ranges.size(); ++k) {
         const CodeRange& r = c->code_ranges[k];
@@ -811,7 +849,9 @@ gcv_status launch_main_pass(gcv_ctx* c, LengthParams P)
         P.list = c->seg_list.p + r.begin;
         P.n_items = r.end - r.begin;
         P.work = c->ctr.p + C_WORK_CODE + k;
+        CHECK(mark(r.code, 0));
         CHECK(launch_length<0>(c, r.code, P));
+        CHECK(mark(r.code, 1));
     }
     return GCV_OK;
 }
@@ -841,7 +881,11 @@ void select_knobs(gcv_ctx* c)
             return;
         }
     }
-    if (c->len_trial >= 0 && c->len_trial < TUNE_TRIALS) c->knobs.length_cap = trial_knobs(c->len_trial).length_cap;
+    if (c->len_trial >= 0 && c->len_trial < TUNE_TRIALS) {
+        const Knobs k = trial_knobs(c->len_trial);
+        std::memcpy(c->knobs.length_cap, k.length_cap, sizeof(k.length_cap));
+        c->knobs.deep_cap = k.deep_cap;
+    }
     if (c->smp_trial >= 0 && c->smp_trial < TUNE_TRIALS) {
         const Knobs k = trial_knobs(c->smp_trial);
         c->knobs.sample_threads = k.sample_threads;
@@ -857,11 +901,28 @@ int argmin3(const double* v)
     return b;
 }
 
+// the length shapes of finished trials: each code its fastest trial, the
+// deep passes the trial with the fastest length phase as a whole
+void choose_length_knobs(gcv_ctx* c, Knobs& k)
+{
+    const int all = argmin3(c->len_ms);
+    for (int sl = 0; sl < N_CODE_SLOTS; ++sl) {
+        double v[TUNE_TRIALS];
+        bool timed = true;
+        for (int i = 0; i < TUNE_TRIALS; ++i) {
+            v[i] = c->len_code_ms[i][sl];
+            timed = timed && v[i] > 0.0;
+        }
+        k.length_cap[sl] = trial_length_cap(timed ? argmin3(v) : all);
+    }
+    k.deep_cap = trial_length_cap(all);
+}
+
 void tune_finish_if_done(gcv_ctx* c)
 {
     if (c->len_trial == TUNE_TRIALS && c->smp_trial == TUNE_TRIALS) {
         Knobs k;
-        k.length_cap = trial_knobs(argmin3(c->len_ms)).length_cap;
+        choose_length_knobs(c, k);
         const Knobs ks = trial_knobs(argmin3(c->smp_ms));
         k.sample_threads = ks.sample_threads;
         k.sample_blocks_per_sm = ks.sample_blocks_per_sm;
@@ -879,9 +940,15 @@ gcv_status tune_after_table(gcv_ctx* c)
     CU(cudaEventSynchronize(c->ev[2]));
     float ms = 0.f;
     CU(cudaEventElapsedTime(&ms, c->ev[6], c->ev[2]));
+    for (int sl = 0; sl < N_CODE_SLOTS; ++sl) {
+        float mc = 0.f;
+        c->len_code_ms[c->len_trial][sl] = 0.0;
+        if (c->code_timed[sl] && cudaEventElapsedTime(&mc, c->ev_code[sl][0], c->ev_code[sl][1]) == cudaSuccess)
+            c->len_code_ms[c->len_trial][sl] = std::max(mc, 1e-6f);
+    }
+    cudaGetLastError();
     c->len_ms[c->len_trial++] = ms;
-    if (c->len_trial == TUNE_TRIALS && c->smp_trial >= 0 && c->smp_trial < TUNE_TRIALS)
-        c->knobs.length_cap = trial_knobs(argmin3(c->len_ms)).length_cap;
+    if (c->len_trial == TUNE_TRIALS && c->smp_trial >= 0 && c->smp_trial < TUNE_TRIALS) choose_length_knobs(c, c->knobs);
     tune_finish_if_done(c);
     return GCV_OK;
 }
@@ -1282,7 +1349,7 @@ gcv_status enqueue_table_graph(gcv_ctx* c)
         P.collect = c->opt.collect_stats;
         P.coef_ff = c->coef_ff.p;
         P.starts = learned ? c->starts.p : nullptr;
-        CHECK(launch_main_pass(c, P));
+        CHECK(launch_main_pass(c, P, true));
         // deep passes over the deep list, its length read on the device
         LengthParams Q = P;
         Q.list = c->deep_list.p;
@@ -1969,7 +2036,8 @@ gcv_status gcv_get_stats(gcv_ctx* ctx, gcv_stats* out)
         }
     }
     cudaGetLastError();
-    ctx->stats.length_blocks_per_sm = ctx->knobs.length_cap;
+    ctx->stats.length_blocks_per_sm = ctx->code >= 0 ? ctx->knobs.length_cap[code_slot(ctx->code)] : ctx->knobs.deep_cap;
+    for (int sl = 0; sl < N_CODE_SLOTS; ++sl) ctx->stats.length_blocks_per_sm_code[sl] = ctx->knobs.length_cap[sl];
     ctx->stats.sample_threads = ctx->knobs.sample_threads;
     ctx->stats.sample_blocks_per_sm = ctx->knobs.sample_blocks_per_sm;
     ctx->stats.tuned = ctx->len_trial < 0 ? 1 : 0;

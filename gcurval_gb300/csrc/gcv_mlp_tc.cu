@@ -243,6 +243,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
     for (int64_t tile = (int64_t)blockIdx.x * NWG + wg; tile < tiles && ok; tile += (int64_t)gridDim.x * NWG) {
         const int64_t row = tile * 128 + t;
         const bool live = row < A.n;
+        // the interval this row's start depths go to, fetched now: its load
+        // latency then hides behind the four layers
+        int64_t out_s = 0;
+        if constexpr (STARTS) out_s = live ? (A.list ? (int64_t)A.list[A.row0 + row] : A.row0 + row) : 0;
         // ---- features -> X (bf16, K-major core matrices, K = 16); the next
         // tile's rows are fetched now and used one iteration later
         if constexpr (BF16IN) {
@@ -322,8 +326,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_mlp_tc(TcArgs A)
                 for (int i = 0; i < 32; ++i) o[i] = __uint_as_float(r[i]) + bias4[i];
                 if (live) {
                     if constexpr (STARTS) {
-                        const int64_t s = A.list ? (int64_t)A.list[A.row0 + row] : A.row0 + row;
-                        A.starts[s] = quarter_depths(o, A.max_depth);
+                        A.starts[out_s] = quarter_depths(o, A.max_depth);
                     } else {
 #pragma unroll
                         for (int i = 0; i < 32; ++i) A.out[row * MLP_OUT + i] = o[i];

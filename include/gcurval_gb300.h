@@ -98,6 +98,8 @@ typedef struct gcv_result {
 
 /* Counters of the last table build / sampling call (filled when
  * options.collect_stats is set; the timings always). */
+#define GCV_N_CODE_SLOTS 11
+
 typedef struct gcv_stats {
     int64_t n_curves;
     int64_t n_segments;       /* knot intervals */
@@ -114,6 +116,9 @@ typedef struct gcv_stats {
        builds and samplings of a batch shape new to the process each try one
        candidate, later ones use the fastest (tuned = 1) */
     int length_blocks_per_sm, sample_threads, sample_blocks_per_sm, tuned;
+    /* persistent length workers per SM of each curve code's main pass, by
+       slot: ellipse 0, degree 1..5 in 2D at 1..5, in 3D at 6..10 */
+    int length_blocks_per_sm_code[GCV_N_CODE_SLOTS];
 } gcv_stats;
 
 const char* gcv_status_string(gcv_status s);
