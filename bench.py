@@ -88,11 +88,17 @@ CPU_SAMPLES = {
 }
 
 
+# Untimed steps before every timed run: the autotuner's four trial table
+# builds of a new batch shape (and form) settle within them.
+TUNED_WARMUP = 5
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=5,
+                    help="untimed steps (at least 5: the autotuner's four trial builds settle first)")
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="uneven_batch")
     ap.add_argument("--precision", choices=["plain", "mixed", "learned"], default="learned",
@@ -386,7 +392,7 @@ class Bench:
         with torch.cuda.stream(self.stream):
             self.flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
-    def run(self, res, prec, steps, warmup, learned_on=False, model=None, clocks=False):
+    def run(self, res, prec, steps, warmup, learned_on=False, model=None, clocks=False, mapping="lane"):
         """Times `steps` table builds + samplings (after `warmup` untimed ones)."""
         import gcurval_gb300 as g
         torch = self.torch
@@ -394,7 +400,7 @@ class Bench:
         with torch.cuda.stream(self.stream):
             calc = g.ArclengthCalculateGpu.from_device_batch(*res.arr, precision=prec, rtol=b.rtol,
                                                              collect_stats=True, learned=learned_on,
-                                                             stream=self.stream)
+                                                             stream=self.stream, mapping=mapping)
             if learned_on:
                 calc.set_learned_model(model)
 
@@ -531,13 +537,13 @@ def measure_config(name, workload, precision, bench, args, fp64_peak, fp32_peak,
     batch = make_batch(workload, seed=0)
     res = Resident(batch, bench.dev)
     prec = g.GCV_PLAIN_FP64 if precision == "plain" else g.GCV_MIXED
-    r = bench.run(res, prec, args.config_steps, 3)
-    plain_r = None if precision == "plain" else bench.run(res, g.GCV_PLAIN_FP64, 2, 1)
+    r = bench.run(res, prec, args.config_steps, TUNED_WARMUP)
+    plain_r = None if precision == "plain" else bench.run(res, g.GCV_PLAIN_FP64, 2, TUNED_WARMUP)
     del res
     value = batch.n_curve / (r["ms_per_step"] * 1e-3)
     out = {"workload": f"{workload}: {WORKLOADS[workload][1]}", "precision": precision, "rtol": batch.rtol,
            "value": round(value, 3), "unit": "curves/s", "ms_per_step": round(r["ms_per_step"], 4),
-           "steps": r["steps"], "warmup": 3,
+           "steps": r["steps"], "warmup": TUNED_WARMUP,
            "samples_per_s": round(batch.total_samples / (r["ms_per_step"] * 1e-3), 1),
            "roofline": roofline_of(batch, r, plain_r, precision == "plain", workload, precision, fp64_peak,
                                    fp32_peak, hbm_peak_gbs())}
@@ -589,14 +595,18 @@ def main():
     # ---- device-resident arm ------------------------------------------------
     bench = Bench(dev, local, dist, use_graph=not args.no_graph)
     res = Resident(batch, dev)
-    main_r = bench.run(res, precision, args.steps, max(args.warmup, 3), learned_on=use_learned, model=model,
+    main_r = bench.run(res, precision, args.steps, max(args.warmup, 5), learned_on=use_learned, model=model,
                        clocks=True)
-    plain_r = mixed_r = None
+    plain_r = mixed_r = hw_r = None
     if precision != g.GCV_PLAIN_FP64 and args.plain_steps > 0:
-        plain_r = bench.run(res, g.GCV_PLAIN_FP64, args.plain_steps, 1)
+        plain_r = bench.run(res, g.GCV_PLAIN_FP64, args.plain_steps, TUNED_WARMUP)
         if use_learned:
             # the same mixed-precision walk without the network: what the network gains
-            mixed_r = bench.run(res, g.GCV_MIXED, args.plain_steps, 1)
+            mixed_r = bench.run(res, g.GCV_MIXED, args.plain_steps, TUNED_WARMUP)
+        if precision == g.GCV_MIXED:
+            # the length walk's other mapping: one half-warp per knot interval
+            hw_r = bench.run(res, precision, args.plain_steps, TUNED_WARMUP, learned_on=use_learned, model=model,
+                             mapping="half_warp")
     del res
     ms_per_step = main_r["ms_per_step"]
     value = job_throughput(n_curves, ms_per_step, world)
@@ -662,7 +672,7 @@ def main():
     if plain_r is not None:
         pv = job_throughput(n_curves, plain_r["ms_per_step"], world)
         plain = {"value": round(pv, 3), "unit": "curves/s", "ms_per_step": round(plain_r["ms_per_step"], 4),
-                 "steps": args.plain_steps, "warmup": 1, "rtol": rtol,
+                 "steps": args.plain_steps, "warmup": TUNED_WARMUP, "rtol": rtol,
                  "samples_per_s": round(world * n_samples / (plain_r["ms_per_step"] * 1e-3), 1),
                  "phases_ms": {"length": round(float(np.mean(plain_r["ms_len"])), 4),
                                "sample": round(float(np.mean(plain_r["ms_samp"])), 4),
@@ -682,10 +692,18 @@ def main():
                 "panels_saved_frac": round(1.0 - float(np.mean(main_r["n_panels"])) / float(np.mean(mixed_r["n_panels"])), 4),
                 "speedup_over_mixed": round(value / mv, 4)}
 
+    mapping_cmp = None
+    if hw_r is not None:
+        ms_l_lane = float(np.mean([a - b for a, b in zip(main_r["ms_len"], main_r["ms_learned"])]))
+        ms_l_hw = float(np.mean([a - b for a, b in zip(hw_r["ms_len"], hw_r["ms_learned"])]))
+        mapping_cmp = {"lane_per_interval": {"length_ms": round(ms_l_lane, 4), "ms_per_step": round(ms_per_step, 4)},
+                       "half_warp_per_interval": {"length_ms": round(ms_l_hw, 4),
+                                                  "ms_per_step": round(hw_r["ms_per_step"], 4)},
+                       "length_speedup_of_lane": round(ms_l_hw / ms_l_lane, 4)}
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "curves/s", "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+            "warmup": max(args.warmup, 5), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if precision == g.GCV_PLAIN_FP64 else ("f32+f64+bf16" if use_learned else "f32+f64"),
             "data": "synthetic: seeded generator (numpy default_rng, seed = rank)",
@@ -707,6 +725,7 @@ def main():
             "accuracy_vs_fp64_oracle": acc,
             "plain_fp64_same_batch": plain,
             "learned_gain": gain,
+            "length_walk_mapping": mapping_cmp,
             "configs": configs,
             "clocks": main_r["clocks"],
         }

@@ -23,12 +23,14 @@ import ctypes
 
 import numpy as np
 
-from ._lib import (GCV_DEVICE, GCV_HOST, GCV_MIXED, GCV_PLAIN_FP64, GCV_RETURN_POINTS, GCV_RETURN_US,
+from ._lib import (GCV_DEVICE, GCV_HOST, GCV_MAP_HALF_WARP, GCV_MAP_LANE, GCV_MIXED, GCV_PLAIN_FP64,
+                   GCV_RETURN_POINTS, GCV_RETURN_US,
                    GcvError, Options, Result, ResultF32, Stats, check, default_options, load,
                    release_cached_memory)
 
 __all__ = ["ArclengthCalculateGpu", "ArclengthReverseResult", "GcvError", "GCV_DEVICE", "GCV_HOST",
-           "GCV_RETURN_US", "GCV_RETURN_POINTS", "GCV_PLAIN_FP64", "GCV_MIXED", "default_options", "load",
+           "GCV_RETURN_US", "GCV_RETURN_POINTS", "GCV_PLAIN_FP64", "GCV_MIXED", "GCV_MAP_LANE", "GCV_MAP_HALF_WARP",
+           "default_options", "load",
            "release_cached_memory"]
 
 _P = ctypes.c_void_p
@@ -157,9 +159,11 @@ class ArclengthCalculateGpu:
     # ---------------------------------------------------------------- makers
     @staticmethod
     def _opts(precision=GCV_PLAIN_FP64, rtol=None, max_depth=None, stream=None, collect_stats=False,
-              learned=False) -> Options:
+              learned=False, mapping=None) -> Options:
         o = default_options(precision)
         o.learned = int(bool(learned))
+        if mapping is not None:
+            o.mapping = {"lane": GCV_MAP_LANE, "half_warp": GCV_MAP_HALF_WARP}.get(mapping, mapping)
         if rtol is not None:
             o.rtol = float(rtol)
         if max_depth is not None:
@@ -251,8 +255,8 @@ class ArclengthCalculateGpu:
 
     # ------------------------------------------------------ reference API
     def set_options(self, precision=GCV_PLAIN_FP64, rtol=None, max_depth=None, stream=None, collect_stats=False,
-                    learned=False):
-        o = self._opts(precision, rtol, max_depth, stream, collect_stats, learned)
+                    learned=False, mapping=None):
+        o = self._opts(precision, rtol, max_depth, stream, collect_stats, learned, mapping)
         check(self._lib.gcv_set_options(self._h, ctypes.byref(o)))
 
     def createArclengthTable(self):

@@ -28,6 +28,9 @@ GCV_RETURN_POINTS = 3
 
 GCV_PLAIN_FP64 = 0
 GCV_MIXED = 1
+# gcv_mapping: the float-float length walk's threads per knot interval
+GCV_MAP_LANE = 0
+GCV_MAP_HALF_WARP = 1
 
 STATUS_NAMES = {0: "GCV_OK", 1: "GCV_ERR_INVALID", 2: "GCV_ERR_CUDA", 3: "GCV_ERR_OUT_OF_MEMORY",
                 4: "GCV_ERR_STATE", 5: "GCV_ERR_OVERFLOW", 6: "GCV_ERR_TIMEOUT", 7: "GCV_ERR_NO_DEVICE"}
@@ -43,7 +46,8 @@ class GcvError(RuntimeError):
 
 class Options(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("max_depth", ctypes.c_int), ("precision", ctypes.c_int),
-                ("stream", _P), ("collect_stats", ctypes.c_int), ("learned", ctypes.c_int)]
+                ("stream", _P), ("collect_stats", ctypes.c_int), ("learned", ctypes.c_int),
+                ("mapping", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):

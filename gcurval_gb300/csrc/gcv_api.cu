@@ -288,8 +288,10 @@ struct Knobs {
 // learned form, log2 of the interval count).  The length walk is timed code
 // by code (its main pass launches once per curve code), so each code of a
 // batch that mixes codes keeps the persistent-worker count that was fastest
-// for it.  The shapes change scheduling only: every result is the same under
-// each.
+// for it.  The shapes change scheduling only: every result is the same
+// under each, bit for bit.  (The half-warp-per-interval mapping of the main
+// pass sums each panel's nodes in another order, so it is a user option,
+// gcv_options.mapping, not a shape the tuner may pick.)
 constexpr int TUNE_TRIALS = 3;
 inline int trial_length_cap(int i) { return i == 1 ? 4 : (i == 2 ? 6 : 32); }
 inline Knobs trial_knobs(int i)
@@ -459,6 +461,8 @@ Table table_view(gcv_ctx* c)
 gcv_status check_options(const gcv_options* o)
 {
     if (!o) return fail(GCV_ERR_INVALID, "options are NULL");
+    if (o->mapping != GCV_MAP_LANE && o->mapping != GCV_MAP_HALF_WARP)
+        return fail(GCV_ERR_INVALID, "mapping must be GCV_MAP_LANE or GCV_MAP_HALF_WARP");
     if (!(o->rtol > 0.0) || !(o->rtol < 1.0)) return fail(GCV_ERR_INVALID, "rtol must be in (0, 1)");
     if (o->max_depth < 1 || o->max_depth > MAX_DEPTH_LIMIT)
         return fail(GCV_ERR_INVALID, "max_depth must be in [1, " + std::to_string(MAX_DEPTH_LIMIT) + "]");
@@ -794,9 +798,12 @@ gcv_status launch_length_code(gcv_ctx* c, int code, const LengthParams& P)
     cudaError_t e = cudaErrorInvalidValue;
     if constexpr (MODE == 0) {
         const int cap = c->knobs.length_cap[code_slot(code)];
+        const bool half_warp = PREC == 1 && c->opt.mapping == GCV_MAP_HALF_WARP;
         switch (code) {
 #define GCV_CASE(C)                                                                                \
-    case C: e = length_launch<0, C, PREC>(P, c->stream, sms, cap); break;
+    case C:                                                                                        \
+        e = half_warp ? length_launch_hw<C>(P, c->stream, sms, cap) : length_launch<0, C, PREC>(P, c->stream, sms, cap); \
+        break;
             GCV_FOR_EACH_CODE(GCV_CASE)
 #undef GCV_CASE
         default: return fail(GCV_ERR_INVALID, "no length kernel for curve code " + std::to_string(code));
@@ -1679,7 +1686,7 @@ gcv_status gcv_set_options(gcv_ctx* ctx, const gcv_options* opt)
     if (!ctx) return fail(GCV_ERR_INVALID, "ctx is NULL");
     CHECK(check_options(opt));
     const bool rebuild = opt->precision != ctx->opt.precision || opt->rtol != ctx->opt.rtol ||
-                         opt->max_depth != ctx->opt.max_depth;
+                         opt->max_depth != ctx->opt.max_depth || opt->mapping != ctx->opt.mapping;
     ctx->opt = *opt;
     ctx->stream = (cudaStream_t)opt->stream;
     if (rebuild) {

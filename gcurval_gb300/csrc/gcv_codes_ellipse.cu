@@ -1,5 +1,5 @@
 // Length-pass and sampling instantiations: ellipses, and the runtime-dispatch deep passes.
-#include "gcv_length_impl.cuh"
+#include "gcv_length_hw.cuh"
 #include "gcv_sample_impl.cuh"
 
 namespace gcv {
@@ -9,4 +9,5 @@ GCV_LENGTH_INST2(2, CODE_ELLIPSE)
 GCV_LENGTH_INST2(1, -1)
 GCV_LENGTH_INST2(2, -1)
 GCV_SAMPLE_INST2(CODE_ELLIPSE)
+GCV_LENGTH_HW_INST(CODE_ELLIPSE)
 }  // namespace gcv

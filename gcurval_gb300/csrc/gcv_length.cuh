@@ -57,4 +57,9 @@ struct LengthParams {
 template <int MODE, int CODE, int PREC>
 cudaError_t length_launch(const LengthParams& P, cudaStream_t stream, int sm_count, int blocks_per_sm_cap);
 
+// The main pass (MODE 0) with float-float panels and one half-warp per knot
+// interval instead of one lane (gcv_length_hw.cuh); same table.
+template <int CODE>
+cudaError_t length_launch_hw(const LengthParams& P, cudaStream_t stream, int sm_count, int blocks_per_sm_cap);
+
 }  // namespace gcv

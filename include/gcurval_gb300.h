@@ -78,7 +78,14 @@ typedef struct gcv_options {
     int learned;          /* nonzero: start B-spline intervals at the depths predicted by the
                              network installed with gcv_set_learned_model
                              (gcurval_gb300_learned.h); no effect without one */
+    int mapping;          /* the length walk's main pass with float-float panels (GCV_MIXED):
+                             GCV_MAP_LANE (default) one thread per knot interval, or
+                             GCV_MAP_HALF_WARP 16 threads per knot interval, one panel node
+                             each; the same table up to the summation order of each
+                             panel's nodes (float-float rounding); no effect on GCV_PLAIN_FP64 */
 } gcv_options;
+
+enum gcv_mapping { GCV_MAP_LANE = 0, GCV_MAP_HALF_WARP = 1 };
 
 typedef struct gcv_ctx gcv_ctx;
 

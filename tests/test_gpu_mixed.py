@@ -111,3 +111,29 @@ def test_mixed_full_size_3d_workload(gpu_lib):
     s = o.s_at(sub.n_samples, usub)
     Lr = np.repeat(Lo, sub.n_samples)
     assert np.max(np.abs(s - sub.sample_positions() * Lr) / Lr) <= RTOL
+
+
+@pytest.mark.parametrize("learned", [False, True])
+def test_half_warp_mapping_builds_the_same_table(learned, gpu_lib):
+    # one half-warp per knot interval (GCV_MAP_HALF_WARP) against one lane per
+    # interval: the same panels and leaves; the nodes of each panel are summed
+    # in another order, so values agree to float-float rounding
+    b = ds.uneven_batch(1500, seed=33, max_ctrl=300, max_samples=64)
+    pos = b.sample_positions()
+    out = {}
+    for mapping in ("lane", "half_warp"):
+        calc = g.ArclengthCalculateGpu.from_batch(b, precision=g.GCV_MIXED, rtol=b.rtol, learned=learned,
+                                                  mapping=mapping, collect_stats=True)
+        if learned:
+            from gcurval_gb300 import learned as lm
+            calc.set_learned_model(lm.load_model())
+        calc.createArclengthTable()
+        L = calc.getAllCurveArclengths()
+        u = calc.arclengthReverse(b.n_samples, pos, True, g.GCV_HOST).us
+        st = calc.stats()
+        calc.close()
+        out[mapping] = (L, u, st["n_panels"], st["n_leaves"])
+    (L0, u0, p0, l0), (L1, u1, p1, l1) = out["lane"], out["half_warp"]
+    assert abs(p1 - p0) <= 1e-3 * p0 and abs(l1 - l0) <= 1e-3 * l0
+    assert np.max(np.abs(L1 - L0) / L0) <= 1e-12
+    assert np.max(np.abs(u1 - u0)) <= 1e-11
