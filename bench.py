@@ -115,6 +115,9 @@ def parse():
     ap.add_argument("--cpu-sample-curves", type=int, default=0,
                     help="curves of the CPU sample at the default tolerance, all threads (0: the workload's default)")
     ap.add_argument("--n-curves", type=int, default=0, help="override the workload's curve count (profiling runs)")
+    ap.add_argument("--split", action="store_true",
+                    help="N > 1: split one batch over the ranks by contiguous curve ranges (strong scaling) "
+                         "instead of one batch per rank")
     return ap.parse_args()
 
 
@@ -586,7 +589,17 @@ def main():
     if use_learned:
         from gcurval_gb300 import learned as _learned
         model = _learned.load_model()
-    batch = make_batch(args.workload, seed=rank, n_curves=args.n_curves)
+    split = args.split and world > 1
+    if split:
+        # one batch, this rank's contiguous share of its curves
+        from gcurval_gb300 import sharding
+        full = make_batch(args.workload, seed=0, n_curves=args.n_curves)
+        _, _, batch = sharding.shard(full, rank, world)
+        job_curves, job_samples = full.n_curve, full.total_samples
+        del full
+    else:
+        batch = make_batch(args.workload, seed=rank, n_curves=args.n_curves)
+        job_curves, job_samples = world * batch.n_curve, world * batch.total_samples
     pos = batch.positions
     n_curves, n_samples = batch.n_curve, batch.total_samples
     rtol = batch.rtol
@@ -609,8 +622,8 @@ def main():
                              mapping="half_warp")
     del res
     ms_per_step = main_r["ms_per_step"]
-    value = job_throughput(n_curves, ms_per_step, world)
-    samples_per_s = world * n_samples / (ms_per_step * 1e-3)
+    value = job_curves / (ms_per_step * 1e-3)
+    samples_per_s = job_samples / (ms_per_step * 1e-3)
     fp64_peak = _lib.measure_fma_peak(0)
     fp32_peak = _lib.measure_fma_peak(1)
     roofline = roofline_of(batch, main_r, plain_r if precision != g.GCV_PLAIN_FP64 else None,
@@ -670,17 +683,17 @@ def main():
                 torch.cuda.empty_cache()
     plain = None
     if plain_r is not None:
-        pv = job_throughput(n_curves, plain_r["ms_per_step"], world)
+        pv = job_curves / (plain_r["ms_per_step"] * 1e-3)
         plain = {"value": round(pv, 3), "unit": "curves/s", "ms_per_step": round(plain_r["ms_per_step"], 4),
                  "steps": args.plain_steps, "warmup": TUNED_WARMUP, "rtol": rtol,
-                 "samples_per_s": round(world * n_samples / (plain_r["ms_per_step"] * 1e-3), 1),
+                 "samples_per_s": round(job_samples / (plain_r["ms_per_step"] * 1e-3), 1),
                  "phases_ms": {"length": round(float(np.mean(plain_r["ms_len"])), 4),
                                "sample": round(float(np.mean(plain_r["ms_samp"])), 4),
                                "setup_scan": round(float(np.mean(plain_r["ms_setup"])), 4)},
                  "speedup_of_this_form": round(value / pv, 3)}
     gain = None
     if mixed_r is not None:
-        mv = job_throughput(n_curves, mixed_r["ms_per_step"], world)
+        mv = job_curves / (mixed_r["ms_per_step"] * 1e-3)
         ms_inf = main_r["ms_learned"]
         gain = {"mixed_without_network": {"value": round(mv, 3), "unit": "curves/s",
                                           "ms_per_step": round(mixed_r["ms_per_step"], 4),
@@ -704,7 +717,7 @@ def main():
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "curves/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 5), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
+            "scaling": "strong" if split else "weak", "vs_baseline": None,
             "dtype": "f64" if precision == g.GCV_PLAIN_FP64 else ("f32+f64+bf16" if use_learned else "f32+f64"),
             "data": "synthetic: seeded generator (numpy default_rng, seed = rank)",
             "config": {"workload": f"{args.workload}: {WORKLOADS[args.workload][1]}",
@@ -713,10 +726,12 @@ def main():
                        "l2": "flushed between timed steps (256 MB write on the step's stream, untimed)",
                        "step": "one captured CUDA graph per step (gcv_step_graph)" if not args.no_graph else
                                "createArclengthTable + arclengthReverseInto",
-                       "parallelism": f"replicas x{world} (independent curves, no collective)"},
+                       "parallelism": (f"split x{world}: contiguous curve ranges of one batch, balanced by cost "
+                                       "(no collective on the data path)") if split else
+                                      f"replicas x{world} (independent curves, no collective)"},
             "samples_per_s": round(samples_per_s, 1),
-            "e2e": {"value": round(world * n_curves / e2e_s, 3), "unit": "curves/s", "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(d2h), "samples_per_s": round(world * n_samples / e2e_s, 1),
+            "e2e": {"value": round(job_curves / e2e_s, 3), "unit": "curves/s", "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h), "samples_per_s": round(job_samples / e2e_s, 1),
                     "ms_per_step": round(e2e_s * 1e3, 3), "breakdown_ms": e2e_parts},
             "gpu_launches": int(main_r["launches"]),
             "launch_shapes": main_r["launch_shapes"],
