@@ -1,6 +1,8 @@
 // The length pass with one half-warp per knot interval (float-float panels):
-// the alternative mapping to k_length's one lane per interval, offered to
-// the autotuner per curve code.
+// the alternative mapping to k_length's one lane per interval, chosen by the
+// caller through gcv_options.mapping (GCV_MAP_HALF_WARP).  It is not an
+// autotuner choice: the two mappings sum K15 and G7 in different orders, and
+// a tuner's choice must leave every result bit-identical.
 //
 // The 16 lanes of a half-warp walk one interval's dyadic panels together:
 // in each panel lane hl evaluates one node (gk_lane: the 15 Kronrod nodes,
