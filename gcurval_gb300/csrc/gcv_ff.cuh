@@ -99,8 +99,18 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b)
 // exact scaling by a power of two
 __device__ __forceinline__ ff ff_scale(ff a, float pow2) { return ff{a.hi * pow2, a.lo * pow2}; }
 
-// a * b + c
-__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) { return ff_add(ff_mul(a, b), c); }
+// a * b + c in one pass: the exact product of the high parts (p + e) and the
+// cross terms enter the sloppy sum with c without first renormalising the
+// product, 15 FP32 instructions instead of ff_add(ff_mul(a, b), c)'s 18,
+// with the same error bound relative to |a b| + |c| (the unnormalised tail t
+// is below 2^-22 |p| and is rounded once more, into the low-order sum).
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c)
+{
+    const float p = __fmul_rn(a.hi, b.hi);
+    const float t = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)));
+    const ff s = two_sum(p, c.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(t, c.lo)));
+}
 
 // 1 / b: y = rcp(b.hi), then one Newton step y + y (1 - b y) with the
 // residual 1 - b y formed by FMAs (b.lo enters there)

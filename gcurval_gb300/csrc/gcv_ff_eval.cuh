@@ -211,9 +211,9 @@ __device__ void bspline_setup_ff(const double* __restrict__ kv, const double* __
                     saved[k] = ff_mul(la, temp[0]);
                 } else {
                     const ff wt = ff_mul(w, temp[k - 1]);
-                    const ff rt = ff_add(ff_mul(ra, temp[k]), ff_neg(wt));
+                    const ff rt = ff_fma(ra, temp[k], ff_neg(wt));
                     N[r][k] = r == 0 ? rt : ff_add(a, rt);
-                    saved[k] = ff_add(ff_mul(la, temp[k]), wt);
+                    saved[k] = ff_fma(la, temp[k], wt);
                 }
             }
         }

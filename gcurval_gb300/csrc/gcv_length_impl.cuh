@@ -83,8 +83,12 @@ __device__ __forceinline__ float chord_of(const T* r)
 
 // PREC 0: FP64 panels; PREC 1: float-float panels (GCV_MIXED), whose K15 /
 // G7 / end values enter the same FP64 bookkeeping (error test, leaf table).
+// The float-float main pass asks for 12 resident blocks per SM (at most 80
+// registers): left to itself the compiler gave degree-4/5 3D 94-96 registers,
+// 10 blocks per SM, where the other codes fit 13 (72 registers, 16 KB of
+// leaf staging per block).
 template <int MODE, int CODE, int PREC = 0>
-__global__ void __launch_bounds__(LK_THREADS) k_length(LengthParams P)
+__global__ void __launch_bounds__(LK_THREADS, (MODE == 0 && PREC == 1) ? 12 : 1) k_length(LengthParams P)
 {
     __shared__ double lf_v[MODE == 0 ? LCAP : 1][LK_THREADS];
     __shared__ double lf_c[MODE == 0 ? LCAP : 1][LK_THREADS];
