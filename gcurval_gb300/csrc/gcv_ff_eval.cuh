@@ -140,6 +140,32 @@ struct EvalFF {
             return ff_sqrt(s);
         }
     }
+    // speed rounded to FP32 and q at a float-float point: the components in
+    // float-float (Horner at the full point), their norm in FP32 (the
+    // sampler's Newton steps use f to FP32 accuracy only)
+    __device__ __forceinline__ static float speed_slope_f(const ff* r, ff v, float& q)
+    {
+        if constexpr (CODE == 0) {
+            return speed_slope(r, v, q).hi;
+        } else {
+            float s = 0.0f, t = 0.0f;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                ff acc = r[(P - 1) * D + d];
+                float dacc = 0.0f;
+#pragma unroll
+                for (int k = P - 2; k >= 0; --k) {
+                    dacc = fmaf(dacc, v.hi, acc.hi);
+                    acc = ff_fma(acc, v, r[k * D + d]);
+                }
+                const float a = acc.hi + acc.lo;
+                s = fmaf(a, a, s);
+                t = fmaf(a, dacc, t);
+            }
+            q = t;
+            return sqrtf(s);
+        }
+    }
     // speed and q in plain FP32 from the coefficients' leading parts: for the
     // leaf table's f and q, which only shape the sampler's initial guess
     __device__ __forceinline__ static float speed_slope32(const ff* r, float v, float& q)
@@ -278,7 +304,7 @@ __device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, 
             const ff dx = ff_scale(ff{c_gk_ff[i].x, c_gk_ff[i].y}, hw);
             const ff s = ff_add(EvalFF<CODE>::speed(r, ff_add(mid, ff_neg(dx))), EvalFF<CODE>::speed(r, ff_add(mid, dx)));
             kk = ff_fma(ff{c_gk_ff[7 + i].x, c_gk_ff[7 + i].y}, s, kk);
-            gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, s, gg);  // weight 0 on Kronrod-only nodes
+            if (i & 1) gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, s, gg);  // the Gauss nodes
         }
     } else {
 #pragma unroll
@@ -377,7 +403,7 @@ __device__ __forceinline__ void panel_k15_ff_pairs(ff* b, unsigned long long k, 
             ff_node_pair<P, D>(b, ff{c_gk_ff[i].x, c_gk_ff[i].y}, ff{c_gk_x2_ff[i].x, c_gk_x2_ff[i].y}, fm, fp);
             const ff sum = ff_add(fm, fp);
             kk = ff_fma(ff{c_gk_ff[7 + i].x, c_gk_ff[7 + i].y}, sum, kk);
-            gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, sum, gg);  // weight 0 on Kronrod-only nodes
+            if (i & 1) gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, sum, gg);  // the Gauss nodes
         }
     } else {
 #pragma unroll

@@ -35,6 +35,57 @@ static __constant__ float2 c_gl8_ff[12] = {
     GCV_FFC(gl8_w(0)),  GCV_FFC(gl8_w(1)),  GCV_FFC(gl8_w(2)),  GCV_FFC(gl8_w(3))};
 #undef GCV_FFC
 
+// Whether the sampler of curve code C takes its Gauss sums by node pairs
+// (gl8_pairs) rather than by evaluating each node: the B-spline codes of
+// degree x dimension below 8.  The larger codes hold more coefficients than
+// their register cap leaves room for beside the pairs' temporaries (100-236
+// bytes of spills at 80-88 registers, and fewer resident warps at 96-104);
+// sampling of the uneven 1M batch took 153.4 ms node by node, 149.2 with
+// pairs for the small codes, 153.1 and 154.6 with pairs for every code at
+// the two register budgets.
+__host__ __device__ constexpr bool sample_node_pairs(int code)
+{
+    return code > 0 && code_degree(code) * code_dim(code) < 8;
+}
+
+// The 8-point Gauss sum over [m - h, m + h] of a B-spline code by symmetric
+// node pairs, as the length walk's panels take theirs: b, the interval's
+// speed coefficients, is shifted in place to m (b[j] = p^(j)(m) / j!), then
+// pair k evaluates the even and odd parts at X = h x_k and returns
+// w_k (f(m - X) + f(m + X)) into the sum (the caller scales it by h).  For
+// degree 5 in 3D that is 30 float-float multiply-adds of shift plus 4 pairs
+// instead of 8 Horner evaluations of 12.
+template <int C, bool UNROLL>
+__device__ __forceinline__ ff gl8_pairs(ff* b, ff m, ff h)
+{
+    constexpr int P = code_degree(C), D = code_dim(C);
+#pragma unroll
+    for (int i = 0; i < P - 1; ++i)
+#pragma unroll
+        for (int j = P - 2; j >= i; --j)
+#pragma unroll
+            for (int d = 0; d < D; ++d) b[j * D + d] = ff_fma(b[(j + 1) * D + d], m, b[j * D + d]);
+    ff I{0.0f, 0.0f};
+    if constexpr (UNROLL) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const ff X = ff_mul(h, to_ff(split_const(gl8_x(k))));
+            ff fm, fp;
+            ff_node_pair<P, D>(b, X, ff_mul(X, X), fm, fp);
+            I = ff_fma(to_ff(split_const(gl8_w(k))), ff_add(fm, fp), I);
+        }
+    } else {
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            const ff X = ff_mul(h, ff{c_gl8_ff[4 + k].x, c_gl8_ff[4 + k].y});
+            ff fm, fp;
+            ff_node_pair<P, D>(b, X, ff_mul(X, X), fm, fp);
+            I = ff_fma(ff{c_gl8_ff[8 + k].x, c_gl8_ff[8 + k].y}, ff_add(fm, fp), I);
+        }
+    }
+    return I;
+}
+
 // UNROLL: small integrands unroll the Gauss loop; large ones (panel_rolled)
 // and the runtime-dispatch kernel keep it rolled, so that the body fits the
 // instruction cache.
@@ -42,13 +93,14 @@ template <int C, bool UNROLL>
 __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg, ff vaf, float dv, ff rl, ff dS,
                                                  float dvg, float eps_s, unsigned long long& newton)
 {
-    ff r[MAX_COEF];
-    EvalFF<C>::load(seg, r);
+    constexpr bool PAIRS = sample_node_pairs(C);
     float blo = 0.0f, bhi = dv;
     ff w{dvg, 0.0f};
     float last = 0.0f;  // the converged Newton step, applied in FP64 at the end
     for (int it = 0; it < NEWTON_MAXIT; ++it) {
         ++newton;
+        ff r[MAX_COEF];
+        EvalFF<C>::load(seg, r);  // every iteration: the node-pair Gauss sum shifts r
         const bool from_left = w.hi <= 0.5f * dv;
         // [a0, a1] in local offsets: [0, w] or [w, dv]
         const ff a0 = from_left ? ff{0.0f, 0.0f} : w;
@@ -56,7 +108,9 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
         const ff h2 = ff_scale(ff_add(a1, ff_neg(a0)), 0.5f);
         const ff m2 = ff_add(ff_add(vaf, a0), h2);
         ff I{0.0f, 0.0f};
-        if constexpr (UNROLL) {
+        if constexpr (PAIRS) {
+            I = gl8_pairs<C, UNROLL>(r, m2, h2);  // r now holds the coefficients about m2
+        } else if constexpr (UNROLL) {
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
                 const ff xk = ff_mul(h2, to_ff(split_const(k < 4 ? -gl8_x(k) : gl8_x(k - 4))));
@@ -78,8 +132,13 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
             blo = w.hi;
         else
             bhi = w.hi;
-        float q0;
-        const float f0 = EvalFF<C>::speed_slope(r, ff_add(vaf, w), q0).hi;
+        // speed at w: after the node-pair sum from the coefficients about m2,
+        // at the end +-h2 of the summed side that is w
+        float q0, f0;
+        if constexpr (PAIRS)
+            f0 = EvalFF<C>::speed_slope_f(r, from_left ? h2 : ff_neg(h2), q0);
+        else
+            f0 = EvalFF<C>::speed_slope_f(r, ff_add(vaf, w), q0);
         const float dn = Fh / f0;
         float step = dn;
         // the second-order step only from a Newton point inside the closed
@@ -89,7 +148,13 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
         const float wn = w.hi - dn;
         if (wn >= blo && wn <= bhi) {
             float q1;
-            const float f1 = EvalFF<C>::speed_slope(r, ff_add(vaf, ff_add_f(w, -dn)), q1).hi;
+            // after the node-pair sum from the coefficients about m2, at the
+            // offset (w - dn) - (a0 + h2) from it; else at va + w - dn
+            float f1;
+            if constexpr (PAIRS)
+                f1 = EvalFF<C>::speed_slope_f(r, ff_add(ff_add_f(w, -dn), ff_neg(ff_add(a0, h2))), q1);
+            else
+                f1 = EvalFF<C>::speed_slope_f(r, ff_add(vaf, ff_add_f(w, -dn)), q1);
             const float d = 2.0f * Fh / (f0 + f1);
             const float s0 = q0 / f0, s1 = q1 / f1;  // f'(w), f'(w - dn)
             const float res = dn * dn * (fabsf(s1 - s0) * (1.0f / 3.0f) + s1 * s1 * fabsf(dn) / (4.0f * f1));
