@@ -13,6 +13,7 @@ arclengthReverse of every sample of every curve.  Prints ONE JSON line (rank 0).
 * ``e2e``      the same metric through the public API with host buffers: context
                creation from host arrays (H2D), table, sampling into host memory
                (H2D positions, D2H parameters), destroy; wall clock per step.
+               The host arrays are page-locked (filled once, before the loop).
 * ``roofline`` for the dominant phase: algorithmic FLOPs (evaluations of the
                plain FP64 method x FLOPs per evaluation as the reference's de
                Boor / ellipse derivative costs them) over the phase's time,
@@ -36,6 +37,7 @@ implementation of the path on this host (rank 0 only).
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import platform
@@ -631,19 +633,24 @@ def main():
                            hbm_peak_gbs())
 
     # ---- end-to-end through the public API with host buffers -----------------
+    # The step's inputs (curve arrays, sample counts and positions) and its
+    # output live in page-locked host memory, filled once before the loop.
     e2e_t, parts = [], []
-    h_out = np.zeros(n_samples, np.float64)
+    hb = dataclasses.replace(batch, **{f: g.pinned_copy(getattr(batch, f)) for f in
+                                       ("kind", "degree", "dim", "knot_off", "knots", "ctrl_off", "ctrl", "n_samples")})
+    h_pos = g.pinned_copy(pos)
+    h_out = g.pinned_empty(n_samples, np.float64)
     for i in range(max(args.e2e_steps, 1) + 1):
         if dist:
             dist.barrier()
         t = [time.perf_counter()]
-        c2 = g.ArclengthCalculateGpu.from_batch(batch, precision=precision, rtol=batch.rtol, learned=use_learned)
+        c2 = g.ArclengthCalculateGpu.from_batch(hb, precision=precision, rtol=batch.rtol, learned=use_learned)
         if use_learned:
             c2.set_learned_model(model)
         t.append(time.perf_counter())
         c2.createArclengthTable()
         t.append(time.perf_counter())
-        c2.arclengthReverseInto(batch.n_samples, pos, h_out, True, g.GCV_RETURN_US)
+        c2.arclengthReverseInto(hb.n_samples, h_pos, h_out, True, g.GCV_RETURN_US)
         t.append(time.perf_counter())
         c2.close()
         t.append(time.perf_counter())
@@ -654,6 +661,7 @@ def main():
     e2e_s = max_over_ranks(float(np.mean(e2e_t)), dist, dev)
     h2d = batch.nbytes() + batch.n_samples.nbytes + pos.nbytes
     d2h = h_out.nbytes
+    del hb, h_pos, h_out
 
     # ---- accuracy, CPU baseline and the other configs (rank 0, N = 1 only) ---
     cpu = acc = None

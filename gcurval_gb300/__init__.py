@@ -25,12 +25,12 @@ import numpy as np
 
 from ._lib import (GCV_DEVICE, GCV_HOST, GCV_MAP_HALF_WARP, GCV_MAP_LANE, GCV_MIXED, GCV_PLAIN_FP64,
                    GCV_RETURN_POINTS, GCV_RETURN_US,
-                   GcvError, Options, Result, ResultF32, Stats, check, default_options, load,
-                   release_cached_memory)
+                   GcvError, Options, Result, ResultF32, Stats, check, default_options, load, pinned_copy,
+                   pinned_empty, release_cached_memory)
 
 __all__ = ["ArclengthCalculateGpu", "ArclengthReverseResult", "GcvError", "GCV_DEVICE", "GCV_HOST",
            "GCV_RETURN_US", "GCV_RETURN_POINTS", "GCV_PLAIN_FP64", "GCV_MIXED", "GCV_MAP_LANE", "GCV_MAP_HALF_WARP",
-           "default_options", "load",
+           "default_options", "load", "pinned_copy", "pinned_empty",
            "release_cached_memory"]
 
 _P = ctypes.c_void_p

@@ -8,6 +8,8 @@ from __future__ import annotations
 import ctypes
 import os
 
+import numpy as np
+
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libgcurval_gb300.so")
 HEADER = os.path.join(os.path.dirname(PKG), "include", "gcurval_gb300.h")
@@ -104,6 +106,8 @@ _SIGS = {
                                      ctypes.POINTER(ctypes.c_int)]),
     "gcv_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     "gcv_release_cached_memory": (ctypes.c_int, [ctypes.POINTER(ctypes.c_int64)]),
+    "gcv_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
+    "gcv_host_free": (ctypes.c_int, [_P]),
     "gcv_step_graph": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, _P]),
     "gcv_step_graph_reset": (ctypes.c_int, [_P]),
     # FP32 data
@@ -190,6 +194,38 @@ def release_cached_memory() -> int:
     n = ctypes.c_int64()
     check(lib.gcv_release_cached_memory(ctypes.byref(n)))
     return n.value
+
+
+class _PinnedBlock:
+    """Page-locked host memory from gcv_host_alloc, exposed to NumPy through
+    the array interface; freed when the last array viewing it goes."""
+
+    def __init__(self, n: int, dtype):
+        self._lib = load()
+        self.dtype = np.dtype(dtype)
+        self.addr = _P()
+        check(self._lib.gcv_host_alloc(ctypes.c_size_t(max(n, 1) * self.dtype.itemsize), ctypes.byref(self.addr)))
+        self.__array_interface__ = {"data": (self.addr.value, False), "shape": (n,), "typestr": self.dtype.str,
+                                    "version": 3}
+
+    def __del__(self):
+        if getattr(self, "addr", None) is not None and self.addr.value:
+            self._lib.gcv_host_free(self.addr)
+            self.addr = None
+
+
+def pinned_empty(n: int, dtype=np.float64) -> np.ndarray:
+    """A 1-D NumPy array of n elements in page-locked host memory: host inputs
+    and outputs in such arrays are copied by the copy engines directly."""
+    return np.asarray(_PinnedBlock(int(n), dtype))
+
+
+def pinned_copy(a) -> np.ndarray:
+    """A page-locked copy of a 1-D array."""
+    a = np.ascontiguousarray(a)
+    out = pinned_empty(a.shape[0], a.dtype)
+    out[...] = a
+    return out
 
 
 def measure_fma_peak(which: int) -> float:

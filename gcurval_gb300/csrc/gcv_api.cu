@@ -1193,11 +1193,25 @@ gcv_status ensure_copy_streams(gcv_ctx* c)
     return GCV_OK;
 }
 
+// Whether host memory at p is page-locked (cudaMallocHost, cudaHostAlloc or
+// cudaHostRegister): the copy engines then move it directly, at the link
+// rate and asynchronously to the host.
+bool host_pinned(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
 // Samples into d_out from positions d_pos.  Host buffers (h_pos, h_out,
-// either may be NULL) are streamed in chunks of curves through pinned
-// staging buffers: while chunk k is sampled, the host threads fill the
-// buffer of chunk k + 1 and drain the results of chunk k - 1, and the copy
-// engines move both over the link.
+// either may be NULL) are streamed in chunks of curves: while chunk k is
+// sampled, the copy engines bring in the positions of chunk k + 1 and take
+// out the results of chunk k - 1.  Page-locked caller buffers are copied
+// directly; pageable ones go through pinned staging buffers that a pool of
+// host threads fills and drains.
 gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, int64_t total, int is_relative,
                         int what, double* d_out, const double* h_pos = nullptr, double* h_out = nullptr)
 {
@@ -1258,15 +1272,21 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, 
         for (int k = 0; k < chunks; ++k)
             max_s = std::max<int64_t>(max_s, c->h_sample_off[(size_t)cut[(size_t)k + 1]] - c->h_sample_off[(size_t)cut[(size_t)k]]);
         CHECK(ensure_copy_streams(c));
-        auto lock = staging_lock();
-        void* slot[STAGE_SLOTS];
-        for (int i = 0; i < STAGE_SLOTS; ++i) {
-            const size_t bytes = (size_t)std::max<int64_t>(max_s, 1) * sizeof(double) * (i < 2 ? 1 : width);
-            cudaError_t e = staging_slot(i, bytes, &slot[i]);
-            if (e != cudaSuccess) return cuda_fail(e, "pinned staging buffer");
+        // page-locked caller buffers are copied directly: no staging, no host copies
+        const bool pin_in = h_pos && host_pinned(h_pos), pin_out = h_out && host_pinned(h_out);
+        std::unique_lock<std::mutex> lock;
+        void* slot[STAGE_SLOTS] = {};
+        if ((h_pos && !pin_in) || (h_out && !pin_out)) {
+            lock = staging_lock();
+            for (int i = 0; i < STAGE_SLOTS; ++i) {
+                if (i < 2 ? !h_pos || pin_in : !h_out || pin_out) continue;
+                const size_t bytes = (size_t)std::max<int64_t>(max_s, 1) * sizeof(double) * (i < 2 ? 1 : width);
+                cudaError_t e = staging_slot(i, bytes, &slot[i]);
+                if (e != cudaSuccess) return cuda_fail(e, "pinned staging buffer");
+            }
         }
         auto s_of = [&](int k) { return c->h_sample_off[(size_t)cut[(size_t)k]]; };
-        auto drain = [&](int k) -> gcv_status {  // results of chunk k -> caller
+        auto drain = [&](int k) -> gcv_status {  // results of chunk k -> caller (staged output only)
             CU(cudaEventSynchronize(c->ev_out[k % STREAM_EVENTS]));
             host_copy(h_out + s_of(k) * width, slot[2 + k % 2], (size_t)(s_of(k + 1) - s_of(k)) * width * sizeof(double));
             return GCV_OK;
@@ -1275,26 +1295,32 @@ gcv_status run_sampling(gcv_ctx* c, const int64_t* d_sample_off, double* d_pos, 
             const int64_t s0 = s_of(k), s1 = s_of(k + 1);
             const int e = k % STREAM_EVENTS;
             if (h_pos && s1 > s0) {
-                if (k >= 2) CU(cudaEventSynchronize(c->ev_in[(k - 2) % STREAM_EVENTS]));  // buffer k % 2 is free
-                host_copy(slot[k % 2], h_pos + s0, (size_t)(s1 - s0) * sizeof(double));
-                CU(cudaMemcpyAsync(d_pos + s0, slot[k % 2], (size_t)(s1 - s0) * sizeof(double), cudaMemcpyHostToDevice,
-                                   c->s_in));
+                const double* src = h_pos + s0;
+                if (!pin_in) {
+                    if (k >= 2) CU(cudaEventSynchronize(c->ev_in[(k - 2) % STREAM_EVENTS]));  // buffer k % 2 is free
+                    host_copy(slot[k % 2], h_pos + s0, (size_t)(s1 - s0) * sizeof(double));
+                    src = (const double*)slot[k % 2];
+                }
+                CU(cudaMemcpyAsync(d_pos + s0, src, (size_t)(s1 - s0) * sizeof(double), cudaMemcpyHostToDevice, c->s_in));
                 CU(cudaEventRecord(c->ev_in[e], c->s_in));
                 CU(cudaStreamWaitEvent(c->stream, c->ev_in[e], 0));
             }
             CHECK(launch_sample_chunk(c, P, cut[(size_t)k], cut[(size_t)k + 1], lo));
             CU(cudaEventRecord(c->ev_done[e], c->stream));
             if (h_out) {
-                // buffer 2 + k % 2 was drained on the host before this point
+                // a staging buffer 2 + k % 2 was drained on the host before this point
                 CU(cudaStreamWaitEvent(c->s_out, c->ev_done[e], 0));
-                CU(cudaMemcpyAsync(slot[2 + k % 2], d_out + s0 * width, (size_t)(s1 - s0) * width * sizeof(double),
+                double* dst = pin_out ? h_out + s0 * width : (double*)slot[2 + k % 2];
+                CU(cudaMemcpyAsync(dst, d_out + s0 * width, (size_t)(s1 - s0) * width * sizeof(double),
                                    cudaMemcpyDeviceToHost, c->s_out));
                 CU(cudaEventRecord(c->ev_out[e], c->s_out));
-                if (k >= 1) CHECK(drain(k - 1));
+                if (k >= 1 && !pin_out) CHECK(drain(k - 1));
             }
         }
-        if (h_out) {
+        if (h_out && !pin_out) {
             CHECK(drain(chunks - 1));
+        } else if (h_out) {
+            CU(cudaStreamSynchronize(c->s_out));
         } else {
             CU(cudaStreamSynchronize(c->s_in));
         }
@@ -2049,6 +2075,23 @@ gcv_status gcv_get_stats(gcv_ctx* ctx, gcv_stats* out)
     ctx->stats.sample_blocks_per_sm = ctx->knobs.sample_blocks_per_sm;
     ctx->stats.tuned = ctx->len_trial < 0 ? 1 : 0;
     *out = ctx->stats;
+    return GCV_OK;
+}
+
+gcv_status gcv_host_alloc(size_t bytes, void** p)
+{
+    if (!p) return fail(GCV_ERR_INVALID, "p is NULL");
+    *p = nullptr;
+    if (bytes == 0) return GCV_OK;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(GCV_ERR_NO_DEVICE, "no CUDA device is available");
+    CU(cudaMallocHost(p, bytes));
+    return GCV_OK;
+}
+
+gcv_status gcv_host_free(void* p)
+{
+    if (p) CU(cudaFreeHost(p));
     return GCV_OK;
 }
 

@@ -258,6 +258,16 @@ gcv_status gcv_measure_fma_peak(int which, double* tflops);
  * buffers of every device; *bytes (may be NULL) receives how many bytes. */
 gcv_status gcv_release_cached_memory(int64_t* bytes);
 
+/* Page-locked host memory for the host-side arrays of gcv_create_batch and
+ * gcv_arclength_reverse_into (curve data, positions, results).  The copy
+ * engines read and write such buffers directly, asynchronously and at the
+ * link rate; pageable arrays are still accepted and are streamed through
+ * the library's own pinned staging buffers by host threads.  *p receives
+ * NULL when bytes is 0.  Free with gcv_host_free.  No reference
+ * counterpart (the reference copies pageable arrays with cudaMemcpy). */
+gcv_status gcv_host_alloc(size_t bytes, void** p);
+gcv_status gcv_host_free(void* p);
+
 /* ---- FP32 data ------------------------------------------------------------
  * The reference's float instantiation, ArclengthCalculateGpu<float> (the
  * samples' default, samples/sample1_ellipse/main.cpp:16-20,

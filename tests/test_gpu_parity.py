@@ -8,6 +8,7 @@ Tolerances (FP64 plain path, rtol 1e-10):
   * against the reference's own sample parameters: |u_gpu - u_ref| within the
     reference's bisection resolution (its table interval / 2^22)
 """
+import dataclasses
 import math
 
 import numpy as np
@@ -326,4 +327,32 @@ def test_host_buffers_stream_in_chunks_like_device_buffers(gpu_lib):
     d_out = torch.empty(b.total_samples, dtype=torch.float64, device="cuda")
     calc.arclengthReverseInto(d_cnt, d_pos, d_out, True, g.GCV_RETURN_US)
     np.testing.assert_array_equal(h_out, d_out.cpu().numpy())
+    # page-locked caller buffers are copied directly, without staging: the
+    # same results, also with only one side page-locked
+    p_pos, p_out = g.pinned_copy(pos), g.pinned_empty(b.total_samples)
+    calc.arclengthReverseInto(b.n_samples, p_pos, p_out, True, g.GCV_RETURN_US)
+    np.testing.assert_array_equal(h_out, p_out)
+    h2 = np.zeros(b.total_samples)
+    calc.arclengthReverseInto(b.n_samples, p_pos, h2, True, g.GCV_RETURN_US)
+    np.testing.assert_array_equal(h_out, h2)
+    p_out[:] = 0.0
+    calc.arclengthReverseInto(b.n_samples, pos, p_out, True, g.GCV_RETURN_US)
+    np.testing.assert_array_equal(h_out, p_out)
     calc.close()
+
+
+def test_create_from_page_locked_arrays(gpu_lib):
+    # a batch whose host arrays are page-locked: the same table and samples
+    b = ds.uneven_batch(3000, seed=12)
+    pb = dataclasses.replace(b, **{f: g.pinned_copy(getattr(b, f)) for f in
+                                   ("kind", "degree", "dim", "knot_off", "knots", "ctrl_off", "ctrl", "n_samples")})
+    pos = b.sample_positions()
+    out = []
+    for bb, pp in ((b, pos), (pb, g.pinned_copy(pos))):
+        with g.ArclengthCalculateGpu.from_batch(bb, precision=g.GCV_MIXED) as calc:
+            calc.createArclengthTable()
+            u = np.zeros(b.total_samples)
+            calc.arclengthReverseInto(bb.n_samples, pp, u, True, g.GCV_RETURN_US)
+            out.append((calc.getAllCurveArclengths(), u))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
