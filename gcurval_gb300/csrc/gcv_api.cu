@@ -1206,6 +1206,20 @@ bool host_pinned(const void* p)
     return a.type == cudaMemoryTypeHost;
 }
 
+// The address under which the GPU reads and writes page-locked host memory
+// at p directly (over the CPU-GPU link, without copies), or NULL when p is
+// not page-locked and mapped.
+void* host_mapped(const void* p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || a.hostPointer != p) return nullptr;
+    return a.devicePointer;
+}
+
 // Samples into d_out from positions d_pos.  Host buffers (h_pos, h_out,
 // either may be NULL) are streamed in chunks of curves: while chunk k is
 // sampled, the copy engines bring in the positions of chunk k + 1 and take
@@ -1592,13 +1606,18 @@ gcv_status gcv_create_batch(gcv_ctx** out, int n_curve, const uint8_t* kind, con
         return fail(GCV_ERR_INVALID, "NULL knots or control array");
     }
     if (where == GCV_HOST) {
-        if ((st = upload(c->kind, hk.data(), hk.size(), c->stream)) != GCV_OK ||
+        // The knots and control points (nearly all of the bytes) go first, on
+        // their own copy stream: from page-locked arrays the copy engines move
+        // them while this thread derives the layout and groups the curves;
+        // the create call still returns only once they have arrived.
+        if ((st = ensure_copy_streams(c)) != GCV_OK || (st = upload(c->knots, knots, (size_t)nk, c->s_in)) != GCV_OK ||
+            (st = upload(c->ctrl, ctrl, (size_t)nc, c->s_in)) != GCV_OK ||
+            (st = upload(c->kind, hk.data(), hk.size(), c->stream)) != GCV_OK ||
             (st = upload(c->degree, hd.data(), hd.size(), c->stream)) != GCV_OK ||
             (st = upload(c->dim, hm.data(), hm.size(), c->stream)) != GCV_OK ||
             (st = upload(c->knot_off, hko.data(), hko.size(), c->stream)) != GCV_OK ||
-            (st = upload(c->ctrl_off, hco.data(), hco.size(), c->stream)) != GCV_OK ||
-            (st = upload(c->knots, knots, (size_t)nk, c->stream)) != GCV_OK ||
-            (st = upload(c->ctrl, ctrl, (size_t)nc, c->stream)) != GCV_OK) {
+            (st = upload(c->ctrl_off, hco.data(), hco.size(), c->stream)) != GCV_OK) {
+            if (c->s_in) cudaStreamSynchronize(c->s_in);
             destroy_ctx(c);
             return st;
         }
@@ -1611,7 +1630,12 @@ gcv_status gcv_create_batch(gcv_ctx** out, int n_curve, const uint8_t* kind, con
         c->knots.borrow(knots, (size_t)nk);
         c->ctrl.borrow(ctrl, (size_t)nc);
     }
-    if ((st = finish_create(c, hk.data(), hd.data(), hm.data(), hko.data(), hco.data(), nullptr)) != GCV_OK) {
+    st = finish_create(c, hk.data(), hd.data(), hm.data(), hko.data(), hco.data(), nullptr);
+    if (where == GCV_HOST) {
+        const cudaError_t e = cudaStreamSynchronize(c->s_in);
+        if (st == GCV_OK && e != cudaSuccess) st = cuda_fail(e, "curve data upload");
+    }
+    if (st != GCV_OK) {
         destroy_ctx(c);
         return st;
     }
@@ -1783,21 +1807,34 @@ gcv_status gcv_arclength_reverse_into(gcv_ctx* ctx, const int* n_ptrs_for_curves
     CHECK(stage_counts(ctx, n_ptrs_for_curves, in_where, &total));
     if (total == 0) return GCV_OK;
     if (!sample_position || !out) return fail(GCV_ERR_INVALID, "NULL positions or output");
-    // host buffers are streamed through device buffers in chunks, overlapped
-    // with the sampling kernels
+    // Page-locked host buffers are read and written by the sampling kernels
+    // in place (each position and result crosses the link once, in the
+    // kernels' own accesses); pageable ones are streamed through device
+    // buffers in chunks, overlapped with the sampling kernels.
     const int width = what == GCV_RETURN_US ? 1 : ctx->point_dim;
+    const double* h_pos = in_where == GCV_HOST ? sample_position : nullptr;
+    double* h_out = out_where == GCV_HOST ? out : nullptr;
     double* d_pos = const_cast<double*>(sample_position);
-    if (in_where == GCV_HOST) {
-        CHECK(ctx->sample_pos.reserve((size_t)total));
-        d_pos = ctx->sample_pos.p;
+    if (h_pos) {
+        if (void* m = host_mapped(h_pos)) {
+            d_pos = (double*)m;
+            h_pos = nullptr;
+        } else {
+            CHECK(ctx->sample_pos.reserve((size_t)total));
+            d_pos = ctx->sample_pos.p;
+        }
     }
     double* d_out = out;
-    if (out_where == GCV_HOST) {
-        CHECK(ctx->sample_out.reserve((size_t)total * width));
-        d_out = ctx->sample_out.p;
+    if (h_out) {
+        if (void* m = host_mapped(h_out)) {
+            d_out = (double*)m;
+            h_out = nullptr;
+        } else {
+            CHECK(ctx->sample_out.reserve((size_t)total * width));
+            d_out = ctx->sample_out.p;
+        }
     }
-    CHECK(run_sampling(ctx, ctx->sample_off.p, d_pos, total, is_relative ? 1 : 0, what, d_out,
-                       in_where == GCV_HOST ? sample_position : nullptr, out_where == GCV_HOST ? out : nullptr));
+    CHECK(run_sampling(ctx, ctx->sample_off.p, d_pos, total, is_relative ? 1 : 0, what, d_out, h_pos, h_out));
     if (out_where == GCV_HOST) CU(cudaStreamSynchronize(ctx->stream));
     return GCV_OK;
 }

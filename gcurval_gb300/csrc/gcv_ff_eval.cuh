@@ -4,6 +4,7 @@
 #pragma once
 
 #include "gcv_ff.cuh"
+#include "gcv_ff2.cuh"
 #include "gcv_table.cuh"
 
 namespace gcv {
@@ -18,56 +19,62 @@ __host__ __device__ constexpr ffc split_const(double x)
 }
 __device__ __forceinline__ ff to_ff(ffc c) { return ff{c.hi, c.lo}; }
 
-// ------------------------------------------------------- sin(pi x), |x| <= 1
-// Reduce x to r in [-1/4, 1/4] with sin(pi x) = +-sin(pi r) or +-cos(pi r),
-// then Taylor series of sin(t), cos(t) in t = pi r (|t| <= pi/4: the 17th /
-// 16th order terms are below 2e-14, far under float-float rounding).
-__device__ __forceinline__ ff ff_sin_taylor(ff t)
+// ------------------------------------------------- sin^2(pi x), |x| <= 1
+// sin^2(pi x) has period 1 and is even: fold x to y in [0, 1/2]; then
+// sin^2(pi y) = S(y) for y <= 1/4 and 1 - S(1/2 - y) above, with S the
+// even series S(u) = sin^2(pi u) = sum_{k >= 1} c_k u^(2k),
+// c_k = (-1)^(k+1) 2^(2k-1) pi^(2k) / (2k)!, for |u| <= 1/4.  Eleven terms:
+// the twelfth is below 1e-19 there, far under float-float rounding.  One
+// series without a branch per node, so that two nodes share one packed
+// evaluation (ff2_sinpi_sq).
+constexpr int SIN2_TERMS = 11;
+__host__ __device__ constexpr double sin2pi_coef(int k)
 {
-    const ff t2 = ff_mul(t, t);
-    // t * (1 - t^2/3! + t^4/5! - ... + t^16/17!)
-    ff p = to_ff(split_const(1.0 / 355687428096000.0));  // 1/17!
-    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 1307674368000.0))));
-    p = ff_fma(p, t2, to_ff(split_const(1.0 / 6227020800.0)));
-    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 39916800.0))));
-    p = ff_fma(p, t2, to_ff(split_const(1.0 / 362880.0)));
-    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 5040.0))));
-    p = ff_fma(p, t2, to_ff(split_const(1.0 / 120.0)));
-    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 6.0))));
-    p = ff_fma(p, t2, ff{1.0f, 0.0f});
-    return ff_mul(p, t);
-}
-__device__ __forceinline__ ff ff_cos_taylor(ff t)
-{
-    const ff t2 = ff_mul(t, t);
-    ff p = to_ff(split_const(1.0 / 20922789888000.0));  // 1/16!
-    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 87178291200.0))));
-    p = ff_fma(p, t2, to_ff(split_const(1.0 / 479001600.0)));
-    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 3628800.0))));
-    p = ff_fma(p, t2, to_ff(split_const(1.0 / 40320.0)));
-    p = ff_fma(p, t2, ff_neg(to_ff(split_const(1.0 / 720.0))));
-    p = ff_fma(p, t2, to_ff(split_const(1.0 / 24.0)));
-    p = ff_fma(p, t2, ff_neg(to_ff(split_const(0.5))));
-    return ff_fma(p, t2, ff{1.0f, 0.0f});
+    double c = 0.5;  // (2 pi)^(2k) / (2k)! / 2
+    for (int i = 1; i <= 2 * k; ++i) c *= 2.0 * PI / i;
+    return (k % 2 == 1) ? c : -c;
 }
 
-// sin(pi x)^2 for x in [-1, 1]
+// x in [-1, 1] -> u in [0, 1/4] and whether the result is 1 - S(u)
+__device__ __forceinline__ ff sinpi_sq_fold(ff x, bool& upper)
+{
+    ff y = x.hi < 0.0f ? ff_neg(x) : x;
+    if (y.hi > 0.5f) y = ff_add_f(ff_neg(y), 1.0f);  // 1 - |x|
+    upper = y.hi > 0.25f;
+    return upper ? ff_add_f(ff_neg(y), 0.5f) : y;
+}
+
+// S(u) = sin^2(pi u), two lanes
+__device__ __forceinline__ ff2 ff2_sin2pi_series(ff2 u)
+{
+    const ff2 U = ff2_mul(u, u);
+    ff2 p = splat(to_ff(split_const(sin2pi_coef(SIN2_TERMS))));
+#pragma unroll
+    for (int k = SIN2_TERMS - 1; k >= 1; --k) p = ff2_fma(p, U, splat(to_ff(split_const(sin2pi_coef(k)))));
+    return ff2_mul(p, U);
+}
+
+// sin^2(pi x) for x in [-1, 1], two lanes
+__device__ __forceinline__ ff2 ff2_sinpi_sq(ff2 x)
+{
+    bool up0, up1;
+    const ff u0 = sinpi_sq_fold(lane0(x), up0), u1 = sinpi_sq_fold(lane1(x), up1);
+    const ff2 S = ff2_sin2pi_series(pack(u0, u1));
+    const ff2 C = ff2_add(splat(ff{1.0f, 0.0f}), ff2_neg(S));
+    return pack(up0 ? lane0(C) : lane0(S), up1 ? lane1(C) : lane1(S));
+}
+
+// sin^2(pi x) for x in [-1, 1]
 __device__ __forceinline__ ff ff_sinpi_sq(ff x)
 {
-    // sin^2(pi x) has period 1 and is even: fold to y in [0, 1/2]
-    float ax = fabsf(x.hi);
-    ff y = x.hi < 0.0f ? ff_neg(x) : x;
-    if (ax > 0.5f) y = ff_add_f(ff_neg(y), 1.0f);  // 1 - |x|
-    (void)ax;
-    // y in [0, 1/2]: sin(pi y) = cos(pi (1/2 - y)); use sin for y <= 1/4
-    const ff pi = to_ff(split_const(3.141592653589793238462643383279502884));
-    ff s;
-    if (y.hi <= 0.25f) {
-        s = ff_sin_taylor(ff_mul(pi, y));
-    } else {
-        s = ff_cos_taylor(ff_mul(pi, ff_add_f(ff_neg(y), 0.5f)));
-    }
-    return ff_mul(s, s);
+    bool up;
+    const ff u = sinpi_sq_fold(x, up);
+    const ff U = ff_mul(u, u);
+    ff p = to_ff(split_const(sin2pi_coef(SIN2_TERMS)));
+#pragma unroll
+    for (int k = SIN2_TERMS - 1; k >= 1; --k) p = ff_fma(p, U, to_ff(split_const(sin2pi_coef(k))));
+    const ff S = ff_mul(p, U);
+    return up ? ff_add_f(ff_neg(S), 1.0f) : S;
 }
 
 // ------------------------------------------------------------- evaluators
@@ -111,6 +118,24 @@ struct EvalFF {
             }
             return ff_sqrt(s);
         }
+    }
+    // the speeds at two points at once (packed lanes): the arithmetic of
+    // speed() lane by lane, each coefficient splat into both lanes
+    __device__ __forceinline__ static ff2 speed2(const ff* r, ff2 v)
+    {
+        if constexpr (CODE == 0) {
+            const ff2 w = ff2_add(ff2_scale(v, (float)ELLIPSE_PIECE_SCALE), splat(ff{r[2].hi, 0.0f}));
+            return ff2_sqrt(ff2_fma(splat(r[0]), ff2_sinpi_sq(w), splat(r[1])));
+        }
+        ff2 s{};
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            ff2 acc = splat(r[(P - 1) * D + d]);
+#pragma unroll
+            for (int k = P - 2; k >= 0; --k) acc = ff2_fma(acc, v, splat(r[k * D + d]));
+            s = d == 0 ? ff2_mul(acc, acc) : ff2_fma(acc, acc, s);
+        }
+        return ff2_sqrt(s);
     }
     // speed and q = f * df/dv (q only to FP32 accuracy: it shapes the initial guess
     // and the stopping test, never the result)
@@ -298,22 +323,14 @@ __device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, 
     const ff fc = EvalFF<CODE>::speed(r, mid);
     ff kk = ff_mul(to_ff(split_const(gk_wk(7))), fc);
     ff gg = ff_mul(to_ff(split_const(gk_wg(7))), fc);
-    if constexpr (panel_rolled<CODE>()) {
+    // the two nodes of a pair in packed lanes
 #pragma unroll 1
-        for (int i = 0; i < 7; ++i) {
-            const ff dx = ff_scale(ff{c_gk_ff[i].x, c_gk_ff[i].y}, hw);
-            const ff s = ff_add(EvalFF<CODE>::speed(r, ff_add(mid, ff_neg(dx))), EvalFF<CODE>::speed(r, ff_add(mid, dx)));
-            kk = ff_fma(ff{c_gk_ff[7 + i].x, c_gk_ff[7 + i].y}, s, kk);
-            if (i & 1) gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, s, gg);  // the Gauss nodes
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < 7; ++i) {
-            const ff dx = ff_scale(to_ff(split_const(gk_x(i))), hw);
-            const ff s = ff_add(EvalFF<CODE>::speed(r, ff_add(mid, ff_neg(dx))), EvalFF<CODE>::speed(r, ff_add(mid, dx)));
-            kk = ff_fma(to_ff(split_const(gk_wk(i))), s, kk);
-            if (i & 1) gg = ff_fma(to_ff(split_const(gk_wg(i))), s, gg);
-        }
+    for (int i = 0; i < 7; ++i) {
+        const ff dx = ff_scale(ff{c_gk_ff[i].x, c_gk_ff[i].y}, hw);
+        const ff2 f = EvalFF<CODE>::speed2(r, pack(ff_add(mid, ff_neg(dx)), ff_add(mid, dx)));
+        const ff s = ff_add(lane0(f), lane1(f));
+        kk = ff_fma(ff{c_gk_ff[7 + i].x, c_gk_ff[7 + i].y}, s, kk);
+        if (i & 1) gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, s, gg);  // the Gauss nodes
     }
     K = ff_scale(kk, hw);
     G = ff_scale(gg, hw);
@@ -331,12 +348,6 @@ __device__ __forceinline__ void panel_k15_ff(const ff* r, unsigned long long k, 
 // in v (2 (P - 1) float-float FMAs per dimension) and the two node
 // positions by about half the work; K15 and G7 are formed as in
 // panel_k15_ff.
-#define GCV_FFC2(x) {split_const(x).hi, split_const(x).lo}
-static __constant__ float2 c_gk_x2_ff[7] = {
-    GCV_FFC2(gk_x(0) * gk_x(0)), GCV_FFC2(gk_x(1) * gk_x(1)), GCV_FFC2(gk_x(2) * gk_x(2)),
-    GCV_FFC2(gk_x(3) * gk_x(3)), GCV_FFC2(gk_x(4) * gk_x(4)), GCV_FFC2(gk_x(5) * gk_x(5)),
-    GCV_FFC2(gk_x(6) * gk_x(6))};
-#undef GCV_FFC2
 
 template <int P, int D>
 __device__ __forceinline__ void ff_node_pair(const ff* b, ff x, ff x2, ff& fm, ff& fp)
@@ -366,6 +377,61 @@ __device__ __forceinline__ void ff_node_pair(const ff* b, ff x, ff x2, ff& fm, f
     fp = ff_sqrt(sp);
 }
 
+// ff_node_pair for two node pairs at once, in the lanes of packed FP32 pairs
+// (FFMA2 / FADD2 / FMUL2): x and x2 hold the two pairs' offsets, the
+// coefficients b are shared (each is splat into both lanes where it is
+// used).  Half the float-float instructions of two ff_node_pair calls, the
+// same roundings lane by lane.
+template <int P, int D>
+__device__ __forceinline__ void ff_node_pair2(const ff* b, ff2 x, ff2 x2, ff2& fm, ff2& fp)
+{
+    constexpr int N = P - 1;
+    constexpr int JE = (N % 2 == 0) ? N : N - 1;
+    constexpr int JO = (N % 2 == 1) ? N : N - 1;
+    ff2 sm{}, sp{};
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        ff2 e = splat(b[JE * D + d]);
+#pragma unroll
+        for (int j = JE - 2; j >= 0; j -= 2) e = ff2_fma(e, x2, splat(b[j * D + d]));
+        ff2 lo_ = e, hi_ = e;
+        if constexpr (JO >= 1) {
+            ff2 o = splat(b[JO * D + d]);
+#pragma unroll
+            for (int j = JO - 2; j >= 1; j -= 2) o = ff2_fma(o, x2, splat(b[j * D + d]));
+            o = ff2_mul(o, x);
+            lo_ = ff2_add(e, ff2_neg(o));
+            hi_ = ff2_add(e, o);
+        }
+        sm = d == 0 ? ff2_mul(lo_, lo_) : ff2_fma(lo_, lo_, sm);
+        sp = d == 0 ? ff2_mul(hi_, hi_) : ff2_fma(hi_, hi_, sp);
+    }
+    fm = ff2_sqrt(sm);
+    fp = ff2_sqrt(sp);
+}
+
+// The seven Kronrod node pairs as four packed steps: step j holds pairs 2j
+// and 2j + 1 (the eighth lane, x = 0 with zero weights, is padding).  Per
+// step: x, x^2, the Kronrod weights and the Gauss weights (zero on the
+// Kronrod-only pairs), each as the hi / lo float pairs of both lanes.
+struct GkStep2 {
+    float2 xh, xl, x2h, x2l, wkh, wkl, wgh, wgl;
+};
+__host__ __device__ constexpr double gk_pair_x(int i) { return i < 7 ? gk_x(i) : 0.0; }
+__host__ __device__ constexpr double gk_pair_wk(int i) { return i < 7 ? gk_wk(i) : 0.0; }
+__host__ __device__ constexpr double gk_pair_wg(int i) { return i < 7 ? gk_wg(i) : 0.0; }
+#define GCV_GK_STEP2(j)                                                                                          \
+    {{split_const(gk_pair_x(2 * j)).hi, split_const(gk_pair_x(2 * j + 1)).hi},                                  \
+     {split_const(gk_pair_x(2 * j)).lo, split_const(gk_pair_x(2 * j + 1)).lo},                                  \
+     {split_const(gk_pair_x(2 * j) * gk_pair_x(2 * j)).hi, split_const(gk_pair_x(2 * j + 1) * gk_pair_x(2 * j + 1)).hi}, \
+     {split_const(gk_pair_x(2 * j) * gk_pair_x(2 * j)).lo, split_const(gk_pair_x(2 * j + 1) * gk_pair_x(2 * j + 1)).lo}, \
+     {split_const(gk_pair_wk(2 * j)).hi, split_const(gk_pair_wk(2 * j + 1)).hi},                                \
+     {split_const(gk_pair_wk(2 * j)).lo, split_const(gk_pair_wk(2 * j + 1)).lo},                                \
+     {split_const(gk_pair_wg(2 * j)).hi, split_const(gk_pair_wg(2 * j + 1)).hi},                                \
+     {split_const(gk_pair_wg(2 * j)).lo, split_const(gk_pair_wg(2 * j + 1)).lo}}
+static __constant__ GkStep2 c_gk_step2[4] = {GCV_GK_STEP2(0), GCV_GK_STEP2(1), GCV_GK_STEP2(2), GCV_GK_STEP2(3)};
+#undef GCV_GK_STEP2
+
 // b: the interval's speed coefficients on entry, shifted in place
 template <int CODE>
 __device__ __forceinline__ void panel_k15_ff_pairs(ff* b, unsigned long long k, int depth, ff& K, ff& G)
@@ -394,27 +460,36 @@ __device__ __forceinline__ void panel_k15_ff_pairs(ff* b, unsigned long long k, 
 #pragma unroll
     for (int d = 0; d < D; ++d) s0 = d == 0 ? ff_mul(b[d], b[d]) : ff_fma(b[d], b[d], s0);
     const ff fc = ff_sqrt(s0);
-    ff kk = ff_mul(to_ff(split_const(gk_wk(7))), fc);
-    ff gg = ff_mul(to_ff(split_const(gk_wg(7))), fc);
+    // the node pairs two at a time in packed lanes; the lanes' sums are
+    // added to the centre's terms at the end
+    ff2 kk2{}, gg2{};
     if constexpr (panel_rolled<CODE>()) {
 #pragma unroll 1
-        for (int i = 0; i < 7; ++i) {
-            ff fm, fp;
-            ff_node_pair<P, D>(b, ff{c_gk_ff[i].x, c_gk_ff[i].y}, ff{c_gk_x2_ff[i].x, c_gk_x2_ff[i].y}, fm, fp);
-            const ff sum = ff_add(fm, fp);
-            kk = ff_fma(ff{c_gk_ff[7 + i].x, c_gk_ff[7 + i].y}, sum, kk);
-            if (i & 1) gg = ff_fma(ff{c_gk_ff[15 + i].x, c_gk_ff[15 + i].y}, sum, gg);  // the Gauss nodes
+        for (int j = 0; j < 4; ++j) {
+            const GkStep2 c = c_gk_step2[j];
+            ff2 fm, fp;
+            ff_node_pair2<P, D>(b, ff2{c.xh, c.xl}, ff2{c.x2h, c.x2l}, fm, fp);
+            const ff2 sum = ff2_add(fm, fp);
+            kk2 = ff2_fma(ff2{c.wkh, c.wkl}, sum, kk2);
+            gg2 = ff2_fma(ff2{c.wgh, c.wgl}, sum, gg2);  // zero weights on the Kronrod-only pairs
         }
     } else {
 #pragma unroll
-        for (int i = 0; i < 7; ++i) {
-            ff fm, fp;
-            ff_node_pair<P, D>(b, to_ff(split_const(gk_x(i))), to_ff(split_const(gk_x(i) * gk_x(i))), fm, fp);
-            const ff sum = ff_add(fm, fp);
-            kk = ff_fma(to_ff(split_const(gk_wk(i))), sum, kk);
-            if (i & 1) gg = ff_fma(to_ff(split_const(gk_wg(i))), sum, gg);
+        for (int j = 0; j < 4; ++j) {
+            const ff2 x = pack(to_ff(split_const(gk_pair_x(2 * j))), to_ff(split_const(gk_pair_x(2 * j + 1))));
+            const ff2 x2 = pack(to_ff(split_const(gk_pair_x(2 * j) * gk_pair_x(2 * j))),
+                                to_ff(split_const(gk_pair_x(2 * j + 1) * gk_pair_x(2 * j + 1))));
+            ff2 fm, fp;
+            ff_node_pair2<P, D>(b, x, x2, fm, fp);
+            const ff2 sum = ff2_add(fm, fp);
+            kk2 = ff2_fma(pack(to_ff(split_const(gk_pair_wk(2 * j))), to_ff(split_const(gk_pair_wk(2 * j + 1)))), sum, kk2);
+            if (j < 3)  // pairs 1, 3, 5 (lane 1) are the Gauss nodes
+                gg2 = ff2_fma(pack(to_ff(split_const(gk_pair_wg(2 * j))), to_ff(split_const(gk_pair_wg(2 * j + 1)))), sum,
+                              gg2);
         }
     }
+    const ff kk = ff_fma(to_ff(split_const(gk_wk(7))), fc, ff_add(lane0(kk2), lane1(kk2)));
+    const ff gg = ff_fma(to_ff(split_const(gk_wg(7))), fc, ff_add(lane0(gg2), lane1(gg2)));
     K = ff_scale(kk, hw);
     G = ff_scale(gg, hw);
 }

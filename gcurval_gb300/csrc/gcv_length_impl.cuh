@@ -81,14 +81,19 @@ __device__ __forceinline__ float chord_of(const T* r)
     return sqrtf(c2);
 }
 
+// Resident blocks per SM the float-float main pass asks for: 12 (at most 80
+// registers).  Left to itself the compiler gave degree-4/5 3D 94-96
+// registers (10 blocks per SM).  With the packed panels the larger codes
+// spill 24-236 bytes at 80 registers, yet the length phase of the uneven 1M
+// batch took 152.1 ms so against 154.0 ms with spill-free per-code caps (10
+// blocks for degree x dimension 8-11, 8 blocks from 12).
+__host__ __device__ constexpr int length_ff_blocks(int) { return 12; }
+
 // PREC 0: FP64 panels; PREC 1: float-float panels (GCV_MIXED), whose K15 /
 // G7 / end values enter the same FP64 bookkeeping (error test, leaf table).
-// The float-float main pass asks for 12 resident blocks per SM (at most 80
-// registers): left to itself the compiler gave degree-4/5 3D 94-96 registers,
-// 10 blocks per SM, where the other codes fit 13 (72 registers, 16 KB of
-// leaf staging per block).
 template <int MODE, int CODE, int PREC = 0>
-__global__ void __launch_bounds__(LK_THREADS, (MODE == 0 && PREC == 1) ? 12 : 1) k_length(LengthParams P)
+__global__ void __launch_bounds__(LK_THREADS, (MODE == 0 && PREC == 1) ? length_ff_blocks(CODE) : 1)
+    k_length(LengthParams P)
 {
     __shared__ double lf_v[MODE == 0 ? LCAP : 1][LK_THREADS];
     __shared__ double lf_c[MODE == 0 ? LCAP : 1][LK_THREADS];

@@ -10,8 +10,8 @@
 // relative length on curves of one or a few knot intervals; float-float can,
 // at a fraction of the FP64 cost on GB300 (FP32:FP64 throughput ~75:1).
 //
-// Ellipse integrands (sin(pi v)) are evaluated with an own float-float
-// sin(pi x) (Taylor series after reduction to |x| <= 1/4).
+// Ellipse integrands (sin^2(pi v)) are evaluated with an own float-float
+// series for sin^2(pi u), |u| <= 1/4, after folding (gcv_ff_eval.cuh).
 #pragma once
 
 #include "gcv_ff_eval.cuh"
@@ -65,25 +65,17 @@ __device__ __forceinline__ ff gl8_pairs(ff* b, ff m, ff h)
         for (int j = P - 2; j >= i; --j)
 #pragma unroll
             for (int d = 0; d < D; ++d) b[j * D + d] = ff_fma(b[(j + 1) * D + d], m, b[j * D + d]);
-    ff I{0.0f, 0.0f};
-    if constexpr (UNROLL) {
+    // pairs (0, 1) and (2, 3) in packed lanes
+    const ff2 h2 = splat(h);
+    ff2 I2{};
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const ff X = ff_mul(h, to_ff(split_const(gl8_x(k))));
-            ff fm, fp;
-            ff_node_pair<P, D>(b, X, ff_mul(X, X), fm, fp);
-            I = ff_fma(to_ff(split_const(gl8_w(k))), ff_add(fm, fp), I);
-        }
-    } else {
-#pragma unroll 1
-        for (int k = 0; k < 4; ++k) {
-            const ff X = ff_mul(h, ff{c_gl8_ff[4 + k].x, c_gl8_ff[4 + k].y});
-            ff fm, fp;
-            ff_node_pair<P, D>(b, X, ff_mul(X, X), fm, fp);
-            I = ff_fma(ff{c_gl8_ff[8 + k].x, c_gl8_ff[8 + k].y}, ff_add(fm, fp), I);
-        }
+    for (int k = 0; k < 4; k += 2) {
+        const ff2 X = ff2_mul(h2, pack(to_ff(split_const(gl8_x(k))), to_ff(split_const(gl8_x(k + 1)))));
+        ff2 fm, fp;
+        ff_node_pair2<P, D>(b, X, ff2_mul(X, X), fm, fp);
+        I2 = ff2_fma(pack(to_ff(split_const(gl8_w(k))), to_ff(split_const(gl8_w(k + 1)))), ff2_add(fm, fp), I2);
     }
-    return I;
+    return ff_add(lane0(I2), lane1(I2));
 }
 
 // UNROLL: small integrands unroll the Gauss loop; large ones (panel_rolled)
@@ -110,17 +102,13 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
         ff I{0.0f, 0.0f};
         if constexpr (PAIRS) {
             I = gl8_pairs<C, UNROLL>(r, m2, h2);  // r now holds the coefficients about m2
-        } else if constexpr (UNROLL) {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-                const ff xk = ff_mul(h2, to_ff(split_const(k < 4 ? -gl8_x(k) : gl8_x(k - 4))));
-                I = ff_fma(to_ff(split_const(gl8_w(k & 3))), EvalFF<C>::speed(r, ff_add(m2, xk)), I);
-            }
         } else {
+            // nodes -x_k and +x_k in packed lanes
 #pragma unroll 1
-            for (int k = 0; k < 8; ++k) {
-                const ff xk = ff_mul(h2, ff{c_gl8_ff[k].x, c_gl8_ff[k].y});
-                I = ff_fma(ff{c_gl8_ff[8 + (k & 3)].x, c_gl8_ff[8 + (k & 3)].y}, EvalFF<C>::speed(r, ff_add(m2, xk)), I);
+            for (int k = 0; k < 4; ++k) {
+                const ff xk = ff_mul(h2, ff{c_gl8_ff[4 + k].x, c_gl8_ff[4 + k].y});
+                const ff2 f = EvalFF<C>::speed2(r, pack(ff_add(m2, ff_neg(xk)), ff_add(m2, xk)));
+                I = ff_fma(ff{c_gl8_ff[8 + k].x, c_gl8_ff[8 + k].y}, ff_add(lane0(f), lane1(f)), I);
             }
         }
         I = ff_mul(I, h2);
@@ -181,10 +169,10 @@ __device__ __forceinline__ double ff_leaf_newton(const float2* __restrict__ seg,
 // final update of v in FP64.
 // Registers per thread are capped (blocks of up to SAMPLE_THREADS_MAX threads
 // still fit): left to itself the compiler gave the degree-4/5 codes 95-117
-// registers, and the occupancy lost cost more than a cap costs.  80 leaves
-// every code spill-free but degree-5 3D, which gets 88 (spill-free there).
-// Sampling of the uneven 1M batch: 215.7 ms uncapped, 203.6 with 80 for
-// every code, 202.6 with 88 for degree-5 3D.
+// registers, and the occupancy lost cost more than a cap costs.  80 (6
+// blocks of 128 threads per SM), 88 for degree-5 3D: with the packed Gauss
+// sums several codes spill 12-88 bytes there, yet sampling of the uneven 1M
+// batch took 139.9 ms, against 143.7 ms with a spill-free 96 (5 blocks).
 __host__ __device__ constexpr int sample_ff_regs(int code) { return code == bs_code(5, 3) ? 88 : 80; }
 static_assert(88 * SAMPLE_THREADS_MAX <= 65536, "a block of SAMPLE_THREADS_MAX must fit one SM");
 template <int CODE>
