@@ -640,25 +640,33 @@ def main():
                                        ("kind", "degree", "dim", "knot_off", "knots", "ctrl_off", "ctrl", "n_samples")})
     h_pos = g.pinned_copy(pos)
     h_out = g.pinned_empty(n_samples, np.float64)
-    for i in range(max(args.e2e_steps, 1) + 1):
-        if dist:
-            dist.barrier()
-        t = [time.perf_counter()]
-        c2 = g.ArclengthCalculateGpu.from_batch(hb, precision=precision, rtol=batch.rtol, learned=use_learned)
-        if use_learned:
-            c2.set_learned_model(model)
-        t.append(time.perf_counter())
-        c2.createArclengthTable()
-        t.append(time.perf_counter())
-        c2.arclengthReverseInto(hb.n_samples, h_pos, h_out, True, g.GCV_RETURN_US)
-        t.append(time.perf_counter())
-        c2.close()
-        t.append(time.perf_counter())
-        if i > 0:
-            e2e_t.append(t[-1] - t[0])
-            parts.append(np.diff(t) * 1e3)
-    e2e_parts = dict(zip(["create", "table", "sample", "destroy"], np.round(np.mean(parts, axis=0), 3).tolist()))
-    e2e_s = max_over_ranks(float(np.mean(e2e_t)), dist, dev)
+    def e2e_steps(in_place):
+        times, split = [], []
+        for i in range(max(args.e2e_steps, 1) + 1):
+            if dist:
+                dist.barrier()
+            t = [time.perf_counter()]
+            c2 = g.ArclengthCalculateGpu.from_batch(hb, precision=precision, rtol=batch.rtol, learned=use_learned,
+                                                    host_in_place=in_place)
+            if use_learned:
+                c2.set_learned_model(model)
+            t.append(time.perf_counter())
+            c2.createArclengthTable()
+            t.append(time.perf_counter())
+            c2.arclengthReverseInto(hb.n_samples, h_pos, h_out, True, g.GCV_RETURN_US)
+            t.append(time.perf_counter())
+            c2.close()
+            t.append(time.perf_counter())
+            if i > 0:
+                times.append(t[-1] - t[0])
+                split.append(np.diff(t) * 1e3)
+        return (max_over_ranks(float(np.mean(times)), dist, dev),
+                dict(zip(["create", "table", "sample", "destroy"], np.round(np.mean(split, axis=0), 3).tolist())))
+
+    # curve arrays read in place by the table build (host_in_place), and
+    # copied to the device at creation
+    e2e_s, e2e_parts = e2e_steps(True)
+    e2e_copy_s, e2e_copy_parts = e2e_steps(False)
     h2d = batch.nbytes() + batch.n_samples.nbytes + pos.nbytes
     d2h = h_out.nbytes
     del hb, h_pos, h_out
@@ -740,7 +748,12 @@ def main():
             "samples_per_s": round(samples_per_s, 1),
             "e2e": {"value": round(job_curves / e2e_s, 3), "unit": "curves/s", "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h), "samples_per_s": round(job_samples / e2e_s, 1),
-                    "ms_per_step": round(e2e_s * 1e3, 3), "breakdown_ms": e2e_parts},
+                    "ms_per_step": round(e2e_s * 1e3, 3), "breakdown_ms": e2e_parts,
+                    "inputs": "page-locked host arrays: curve data read in place by the table build "
+                              "(host_in_place), positions and parameters by the sampling kernels",
+                    "copying_create": {"value": round(job_curves / e2e_copy_s, 3),
+                                       "ms_per_step": round(e2e_copy_s * 1e3, 3),
+                                       "breakdown_ms": e2e_copy_parts}},
             "gpu_launches": int(main_r["launches"]),
             "launch_shapes": main_r["launch_shapes"],
             "roofline": roofline,

@@ -159,9 +159,10 @@ class ArclengthCalculateGpu:
     # ---------------------------------------------------------------- makers
     @staticmethod
     def _opts(precision=GCV_PLAIN_FP64, rtol=None, max_depth=None, stream=None, collect_stats=False,
-              learned=False, mapping=None) -> Options:
+              learned=False, mapping=None, host_in_place=False) -> Options:
         o = default_options(precision)
         o.learned = int(bool(learned))
+        o.host_in_place = int(bool(host_in_place))
         if mapping is not None:
             o.mapping = {"lane": GCV_MAP_LANE, "half_warp": GCV_MAP_HALF_WARP}.get(mapping, mapping)
         if rtol is not None:
@@ -209,7 +210,10 @@ class ArclengthCalculateGpu:
 
     @classmethod
     def from_batch(cls, batch, **kw):
-        """Any CurveBatch (gcurval_gb300.datasets) through gcv_create_batch."""
+        """Any CurveBatch (gcurval_gb300.datasets) through gcv_create_batch.
+        host_in_place=True: page-locked knot and control arrays (pinned_copy)
+        are read in place by every table build instead of being copied; the
+        context keeps references to them."""
         lib = load()
         arrs = (np.ascontiguousarray(batch.kind, np.uint8), np.ascontiguousarray(batch.degree, np.uint8),
                 np.ascontiguousarray(batch.dim, np.uint8), np.ascontiguousarray(batch.knot_off, np.int64),
@@ -218,7 +222,7 @@ class ArclengthCalculateGpu:
         h = _P()
         o = cls._opts(**kw)
         check(lib.gcv_create_batch(ctypes.byref(h), batch.n_curve, *[_ptr(x) for x in arrs], GCV_HOST, ctypes.byref(o)))
-        return cls(h)
+        return cls(h, keep=arrs if o.host_in_place else ())
 
     @classmethod
     def from_device_batch(cls, kind, degree, dim, knot_off, knots, ctrl_off, ctrl, **kw):

@@ -49,7 +49,7 @@ class GcvError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("rtol", ctypes.c_double), ("max_depth", ctypes.c_int), ("precision", ctypes.c_int),
                 ("stream", _P), ("collect_stats", ctypes.c_int), ("learned", ctypes.c_int),
-                ("mapping", ctypes.c_int)]
+                ("mapping", ctypes.c_int), ("host_in_place", ctypes.c_int)]
 
 
 class Result(ctypes.Structure):

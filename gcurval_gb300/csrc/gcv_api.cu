@@ -1605,13 +1605,19 @@ gcv_status gcv_create_batch(gcv_ctx** out, int n_curve, const uint8_t* kind, con
         destroy_ctx(c);
         return fail(GCV_ERR_INVALID, "NULL knots or control array");
     }
+    // page-locked knot and control arrays read in place (opt.host_in_place)
+    void* in_knots = where == GCV_HOST && c->opt.host_in_place && nk > 0 ? host_mapped(knots) : nullptr;
+    void* in_ctrl = where == GCV_HOST && c->opt.host_in_place && nc > 0 ? host_mapped(ctrl) : nullptr;
+    if (in_knots) c->knots.borrow((const double*)in_knots, (size_t)nk);
+    if (in_ctrl) c->ctrl.borrow((const double*)in_ctrl, (size_t)nc);
     if (where == GCV_HOST) {
         // The knots and control points (nearly all of the bytes) go first, on
         // their own copy stream: from page-locked arrays the copy engines move
         // them while this thread derives the layout and groups the curves;
         // the create call still returns only once they have arrived.
-        if ((st = ensure_copy_streams(c)) != GCV_OK || (st = upload(c->knots, knots, (size_t)nk, c->s_in)) != GCV_OK ||
-            (st = upload(c->ctrl, ctrl, (size_t)nc, c->s_in)) != GCV_OK ||
+        if ((st = ensure_copy_streams(c)) != GCV_OK ||
+            (!in_knots && (st = upload(c->knots, knots, (size_t)nk, c->s_in)) != GCV_OK) ||
+            (!in_ctrl && (st = upload(c->ctrl, ctrl, (size_t)nc, c->s_in)) != GCV_OK) ||
             (st = upload(c->kind, hk.data(), hk.size(), c->stream)) != GCV_OK ||
             (st = upload(c->degree, hd.data(), hd.size(), c->stream)) != GCV_OK ||
             (st = upload(c->dim, hm.data(), hm.size(), c->stream)) != GCV_OK ||

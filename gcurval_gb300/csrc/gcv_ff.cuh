@@ -50,6 +50,18 @@ __device__ __forceinline__ ff ff_from_double(double x)
 
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
+// double -> float by truncation of the significand, from the bit pattern
+// (integer operations only), for scale factors that need a few digits;
+// outside the normal float range (and for 0, NaN, Inf) the FP64 conversion
+__device__ __forceinline__ float f32_of_f64_trunc(double x)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned top = (unsigned)(b >> 32);
+    const int e = (int)((top >> 20) & 0x7FFu) - 1023 + 127;
+    if (e <= 0 || e >= 255) return __double2float_rn(x);
+    return __uint_as_float((top & 0x80000000u) | ((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7FFFFFull));
+}
+
 // Knuth TwoSum: s + e == a + b exactly
 __device__ __forceinline__ ff two_sum(float a, float b)
 {

@@ -224,7 +224,8 @@ struct EvalFF {
 // for the mixed path: the same polynomial recursion in v on the FP32 pipes.
 // FP64 is used only to centre the data: knots relative to the span midpoint
 // m and control points relative to the first one of the span (differences
-// that carry the cancellation), each converted once to float-float.
+// that carry the cancellation), each converted once to float-float.  The
+// constant term (the position at the midpoint) is formed in float-float.
 template <int P, int D>
 __device__ void bspline_setup_ff(const double* __restrict__ kv, const double* __restrict__ cp, int span, float2* out)
 {
@@ -284,7 +285,9 @@ __device__ void bspline_setup_ff(const double* __restrict__ kv, const double* __
             ff acc{0.0f, 0.0f};
 #pragma unroll
             for (int i = 1; i <= P; ++i) acc = i == 1 ? ff_mul(dp[0], N[1][k]) : ff_fma(dp[i - 1], N[i][k], acc);
-            if (k == 0) acc = ff_from_double(q + ff_to_double(acc));
+            // the position at the midpoint, P_0 + acc, in float-float (it
+            // only enters points, never the speed)
+            if (k == 0) acc = ff_add(ff_from_double(q), acc);
             out[k * D + d] = make_float2(acc.hi, acc.lo);
         }
     }

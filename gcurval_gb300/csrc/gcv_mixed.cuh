@@ -222,17 +222,25 @@ __global__ void __maxnreg__(sample_ff_regs(CODE)) k_sample_ff(SampleParams P, co
                 const int cnt = t.leaf_cnt[s];
                 int64_t j = lower_bound_key(t.leaf_cum, lo, lo + cnt, dkey(rr)) - lo;
                 if (j >= cnt) j = cnt - 1;
-                const double base = j ? t.leaf_cum[lo + j - 1] : 0.0;
-                const double va = j ? t.leaf_v[lo + j - 1] : -1.0;
-                const float fa = j ? t.leaf_f[lo + j - 1] : (float)t.seg_f0[s];
-                const float qa = j ? t.leaf_q[lo + j - 1] : (float)t.seg_q0[s];
+                double base = 0.0, va = -1.0;
+                float fa, qa;
+                if (j) {
+                    base = t.leaf_cum[lo + j - 1];
+                    va = t.leaf_v[lo + j - 1];
+                    fa = t.leaf_f[lo + j - 1];
+                    qa = t.leaf_q[lo + j - 1];
+                } else {  // the interval's start: its FP64 end values, converted once
+                    fa = (float)t.seg_f0[s];
+                    qa = (float)t.seg_q0[s];
+                }
                 const double vb = t.leaf_v[lo + j];
                 const double cb = t.leaf_cum[lo + j];
                 const float fb = (float)t.leaf_f[lo + j];
                 const float qb = (float)t.leaf_q[lo + j];
                 const ff rl = ff_from_double(rr - base);   // target inside the leaf
                 const ff dS = ff_from_double(cb - base);   // leaf length
-                const float dv = (float)(vb - va);          // leaf width (exact dyadic)
+                const double dvd = vb - va;                 // leaf width (exact dyadic)
+                const float dv = (float)dvd;
                 const ff vaf = ff_from_double(va);
                 // quintic Hermite guess of v(S) on the leaf (FP32)
                 float sig = dS.hi > 0.0f ? rl.hi / dS.hi : 0.0f;
@@ -252,7 +260,7 @@ __global__ void __maxnreg__(sample_ff_regs(CODE)) k_sample_ff(SampleParams P, co
                     dvg = fminf(fmaxf(dvg, 0.0f), dv);
                 }
                 const float2* seg = coef_ff + b.coef_off[c] + (s - s0) * code_stride(code);
-                const float eps_s = P.eps_frac * (float)L;
+                const float eps_s = P.eps_frac * f32_of_f64_trunc(L);
                 double wfinal;
                 if constexpr (CODE >= 0) {
                     wfinal = ff_leaf_newton<(CODE >= 0 ? CODE : 0), !panel_rolled<(CODE >= 0 ? CODE : 0)>()>(
@@ -266,7 +274,14 @@ __global__ void __maxnreg__(sample_ff_regs(CODE)) k_sample_ff(SampleParams P, co
                     default: wfinal = dvg; break;
                     }
                 }
-                v = fmin(fmax(va + wfinal, va), vb);
+                // the offset clamped to [0, dv] on the bit patterns (both
+                // non-negative there; a negative offset or NaN has its sign
+                // bit set or the largest pattern): integer compares, off the
+                // FP64 pipe, as fmin / fmax would clamp it
+                const long long wb = __double_as_longlong(wfinal);
+                if (wb < 0) wfinal = 0.0;
+                else if (wb > __double_as_longlong(dvd)) wfinal = dvd;
+                v = va + wfinal;
             }
         }
         if (P.what == 2) {
@@ -275,7 +290,8 @@ __global__ void __maxnreg__(sample_ff_regs(CODE)) k_sample_ff(SampleParams P, co
                 u = b.kind[c] == 0 ? 0.0 : b.knots[b.knot_off[c] + b.degree[c]];
             } else {
                 const double t0 = t.seg_t0[s], t1 = t.seg_t1[s], hw = 0.5 * (t1 - t0);
-                u = v <= 0.0 ? fma(v + 1.0, hw, t0) : fma(v - 1.0, hw, t1);
+                // v <= 0 on the bit pattern (-0 and negatives have the sign bit)
+                u = __double_as_longlong(v) <= 0 ? fma(v + 1.0, hw, t0) : fma(v - 1.0, hw, t1);
             }
             P.out[i] = u;
         } else {

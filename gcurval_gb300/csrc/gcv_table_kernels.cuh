@@ -30,7 +30,8 @@ __device__ void setup_bspline_seg_ff(const Batch& b, const Table& t, int64_t s, 
         ff r[P * D];
         float q0;
         EvalFF<bs_code(P, D)>::load(at, r);
-        t.seg_f0[s] = ff_to_double(EvalFF<bs_code(P, D)>::speed_slope(r, ff{-1.0f, 0.0f}, q0));
+        // the start speed and slope only shape the sampler's first guess: FP32
+        t.seg_f0[s] = (double)EvalFF<bs_code(P, D)>::speed_slope32(r, -1.0f, q0);
         t.seg_q0[s] = (double)q0;
     } else {
 #pragma unroll

@@ -83,6 +83,11 @@ typedef struct gcv_options {
                              GCV_MAP_HALF_WARP 16 threads per knot interval, one panel node
                              each; the same table up to the summation order of each
                              panel's nodes (float-float rounding); no effect on GCV_PLAIN_FP64 */
+    int host_in_place;    /* nonzero: gcv_create_batch with GCV_HOST does not copy page-locked
+                             knot and control arrays (gcv_host_alloc, cudaMallocHost,
+                             cudaHostRegister); every table build reads them in place over the
+                             CPU-GPU link, so they must stay alive and unchanged for the life
+                             of the context.  Pageable arrays are copied as without it. */
 } gcv_options;
 
 enum gcv_mapping { GCV_MAP_LANE = 0, GCV_MAP_HALF_WARP = 1 };

@@ -348,11 +348,14 @@ def test_create_from_page_locked_arrays(gpu_lib):
                                    ("kind", "degree", "dim", "knot_off", "knots", "ctrl_off", "ctrl", "n_samples")})
     pos = b.sample_positions()
     out = []
-    for bb, pp in ((b, pos), (pb, g.pinned_copy(pos))):
-        with g.ArclengthCalculateGpu.from_batch(bb, precision=g.GCV_MIXED) as calc:
-            calc.createArclengthTable()
+    # copied from pageable arrays, copied from page-locked ones, read in place
+    for bb, pp, in_place in ((b, pos, False), (pb, g.pinned_copy(pos), False), (pb, g.pinned_copy(pos), True)):
+        with g.ArclengthCalculateGpu.from_batch(bb, precision=g.GCV_MIXED, host_in_place=in_place) as calc:
+            for _ in range(2):  # a second table build reads the arrays again
+                calc.createArclengthTable()
             u = np.zeros(b.total_samples)
             calc.arclengthReverseInto(bb.n_samples, pp, u, True, g.GCV_RETURN_US)
             out.append((calc.getAllCurveArclengths(), u))
-    np.testing.assert_array_equal(out[0][0], out[1][0])
-    np.testing.assert_array_equal(out[0][1], out[1][1])
+    for k in (1, 2):
+        np.testing.assert_array_equal(out[0][0], out[k][0])
+        np.testing.assert_array_equal(out[0][1], out[k][1])
