@@ -413,16 +413,18 @@ __device__ __forceinline__ void ff_node_pair2(const ff* b, ff2 x, ff2 x2, ff2& f
     fp = ff2_sqrt(sp);
 }
 
-// The seven Kronrod node pairs as four packed steps: step j holds pairs 2j
-// and 2j + 1 (the eighth lane, x = 0 with zero weights, is padding).  Per
-// step: x, x^2, the Kronrod weights and the Gauss weights (zero on the
-// Kronrod-only pairs), each as the hi / lo float pairs of both lanes.
+// The seven Kronrod node pairs and the centre as four packed steps: step j
+// holds pairs 2j and 2j + 1, and the eighth lane is the centre node (x = 0:
+// both of its "nodes" are the centre, so it carries half the centre
+// weights).  Per step: x, x^2, the Kronrod weights and the Gauss weights
+// (zero on the Kronrod-only pairs), each as the hi / lo float pairs of both
+// lanes.
 struct GkStep2 {
     float2 xh, xl, x2h, x2l, wkh, wkl, wgh, wgl;
 };
 __host__ __device__ constexpr double gk_pair_x(int i) { return i < 7 ? gk_x(i) : 0.0; }
-__host__ __device__ constexpr double gk_pair_wk(int i) { return i < 7 ? gk_wk(i) : 0.0; }
-__host__ __device__ constexpr double gk_pair_wg(int i) { return i < 7 ? gk_wg(i) : 0.0; }
+__host__ __device__ constexpr double gk_pair_wk(int i) { return i < 7 ? gk_wk(i) : 0.5 * gk_wk(7); }
+__host__ __device__ constexpr double gk_pair_wg(int i) { return i < 7 ? gk_wg(i) : 0.5 * gk_wg(7); }
 #define GCV_GK_STEP2(j)                                                                                          \
     {{split_const(gk_pair_x(2 * j)).hi, split_const(gk_pair_x(2 * j + 1)).hi},                                  \
      {split_const(gk_pair_x(2 * j)).lo, split_const(gk_pair_x(2 * j + 1)).lo},                                  \
@@ -459,12 +461,8 @@ __device__ __forceinline__ void panel_k15_ff_pairs(ff* b, unsigned long long k, 
         for (int d = 0; d < D; ++d) b[j * D + d] = ff_scale(b[j * D + d], sc);
         sc *= hw;
     }
-    ff s0{0.0f, 0.0f};
-#pragma unroll
-    for (int d = 0; d < D; ++d) s0 = d == 0 ? ff_mul(b[d], b[d]) : ff_fma(b[d], b[d], s0);
-    const ff fc = ff_sqrt(s0);
-    // the node pairs two at a time in packed lanes; the lanes' sums are
-    // added to the centre's terms at the end
+    // the node pairs two at a time in packed lanes (the centre in the last
+    // step's second lane); the two lanes' sums are added at the end
     ff2 kk2{}, gg2{};
     if constexpr (panel_rolled<CODE>()) {
 #pragma unroll 1
@@ -486,13 +484,13 @@ __device__ __forceinline__ void panel_k15_ff_pairs(ff* b, unsigned long long k, 
             ff_node_pair2<P, D>(b, x, x2, fm, fp);
             const ff2 sum = ff2_add(fm, fp);
             kk2 = ff2_fma(pack(to_ff(split_const(gk_pair_wk(2 * j))), to_ff(split_const(gk_pair_wk(2 * j + 1)))), sum, kk2);
-            if (j < 3)  // pairs 1, 3, 5 (lane 1) are the Gauss nodes
-                gg2 = ff2_fma(pack(to_ff(split_const(gk_pair_wg(2 * j))), to_ff(split_const(gk_pair_wg(2 * j + 1)))), sum,
-                              gg2);
+            // the Gauss nodes: pairs 1, 3, 5 and the centre (lane 1)
+            gg2 = ff2_fma(pack(to_ff(split_const(gk_pair_wg(2 * j))), to_ff(split_const(gk_pair_wg(2 * j + 1)))), sum,
+                          gg2);
         }
     }
-    const ff kk = ff_fma(to_ff(split_const(gk_wk(7))), fc, ff_add(lane0(kk2), lane1(kk2)));
-    const ff gg = ff_fma(to_ff(split_const(gk_wg(7))), fc, ff_add(lane0(gg2), lane1(gg2)));
+    const ff kk = ff_add(lane0(kk2), lane1(kk2));
+    const ff gg = ff_add(lane0(gg2), lane1(gg2));
     K = ff_scale(kk, hw);
     G = ff_scale(gg, hw);
 }
