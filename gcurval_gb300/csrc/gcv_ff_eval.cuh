@@ -83,7 +83,8 @@ struct EvalFF {
     static constexpr int P = code_degree(CODE);
     static constexpr int D = code_dim(CODE);
     // A, B, w0 (ellipse piece) or the derivative polynomial
-    // b[k][d] = (k + 1) a[k + 1][d] of the stored float-float position polynomial a
+    // b[k][d] = (k + 1) a[k + 1][d], stored after the midpoint position a[0]
+    // (bspline_setup_ff)
     __device__ __forceinline__ static void load(const float2* __restrict__ seg, ff* r)
     {
         if constexpr (CODE == 0) {
@@ -92,12 +93,10 @@ struct EvalFF {
             r[2] = ff{seg[2].x, seg[2].y};  // w0 = (2 j + 1) / ELLIPSE_PIECES - 1: exact in FP32
         } else {
 #pragma unroll
-            for (int k = 0; k < P; ++k)
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    const float2 c = seg[(k + 1) * D + d];
-                    r[k * D + d] = k == 0 ? ff{c.x, c.y} : ff_mul_f(ff{c.x, c.y}, float(k + 1));
-                }
+            for (int k = 0; k < P * D; ++k) {
+                const float2 c = seg[D + k];
+                r[k] = ff{c.x, c.y};
+            }
         }
     }
     __device__ __forceinline__ static ff speed(const ff* r, ff v)
@@ -286,8 +285,13 @@ __device__ void bspline_setup_ff(const double* __restrict__ kv, const double* __
 #pragma unroll
             for (int i = 1; i <= P; ++i) acc = i == 1 ? ff_mul(dp[0], N[1][k]) : ff_fma(dp[i - 1], N[i][k], acc);
             // the position at the midpoint, P_0 + acc, in float-float (it
-            // only enters points, never the speed)
-            if (k == 0) acc = ff_add(ff_from_double(q), acc);
+            // only enters points, never the speed); the higher terms are
+            // stored as the derivative's coefficients k a_k, which the walk
+            // and the sampler read without rescaling
+            if (k == 0)
+                acc = ff_add(ff_from_double(q), acc);
+            else if (k > 1)
+                acc = ff_mul_f(acc, float(k));
             out[k * D + d] = make_float2(acc.hi, acc.lo);
         }
     }

@@ -298,10 +298,14 @@ __global__ void __maxnreg__(sample_ff_regs(CODE)) k_sample_ff(SampleParams P, co
             double p3[3] = {0.0, 0.0, 0.0};
             if (s >= 0) {
                 // points from the float-float coefficients, evaluated in FP64
+                // (a B-spline stores a[0] and then b[k - 1] = k a[k])
                 const float2* seg = coef_ff + b.coef_off[c] + (s - s0) * code_stride(code);
                 double cd[MAX_COEF];
-                const int n = code_stride(code);
-                for (int k = 0; k < n; ++k) cd[k] = (double)seg[k].x + (double)seg[k].y;
+                const int n = code_stride(code), dim = code_dim(code);
+                for (int k = 0; k < n; ++k) {
+                    cd[k] = (double)seg[k].x + (double)seg[k].y;
+                    if (code != 0 && k >= 2 * dim) cd[k] *= 1.0 / (double)(k / dim);
+                }
                 if constexpr (CODE >= 0)
                     Eval<(CODE >= 0 ? CODE : 0)>::point(cd, v, p3);
                 else
