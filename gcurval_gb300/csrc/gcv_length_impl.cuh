@@ -81,13 +81,16 @@ __device__ __forceinline__ float chord_of(const T* r)
     return sqrtf(c2);
 }
 
-// Resident blocks per SM the float-float main pass asks for: 12 (at most 80
-// registers).  Left to itself the compiler gave degree-4/5 3D 94-96
-// registers (10 blocks per SM).  With the packed panels the larger codes
-// spill 24-236 bytes at 80 registers, yet the length phase of the uneven 1M
-// batch took 152.1 ms so against 154.0 ms with spill-free per-code caps (10
-// blocks for degree x dimension 8-11, 8 blocks from 12).
-__host__ __device__ constexpr int length_ff_blocks(int) { return 12; }
+// Resident blocks per SM the float-float main pass asks for, per curve code:
+// 10 (at most 96 registers) for degree 3-5 in 3D, 12 (80) for the others.
+// Single-code batches of the uneven 100k batch, main pass alone, at 12 / 10 /
+// 8 blocks: degree 2-3 in 2D and degree 2 in 3D are fastest at 12 (3-14 %
+// ahead of 8), degree 4-5 in 2D tie at 12 and 10, degree 3-5 in 3D gain 2-4 %
+// at 10 (they spill 112-216 bytes at 80 registers, less at 96).
+__host__ __device__ constexpr int length_ff_blocks(int code)
+{
+    return code > 0 && code_dim(code) == 3 && code_degree(code) >= 3 ? 10 : 12;
+}
 
 // PREC 0: FP64 panels; PREC 1: float-float panels (GCV_MIXED), whose K15 /
 // G7 / end values enter the same FP64 bookkeeping (error test, leaf table).
@@ -335,33 +338,54 @@ __global__ void __launch_bounds__(LK_THREADS, (MODE == 0 && PREC == 1) ? length_
                 unsigned long long base = 0;
                 if (lane == 0) base = atomicAdd(t.ctr + C_LEAF_TOP, (unsigned long long)total);
                 base = __shfl_sync(FULL, base, 0);
-                if (fin) {
-                    const int64_t off = (int64_t)base + incl - x;
-                    if (off + nleaf <= t.leaf_cap) {
-                        if constexpr (PREC == 1) {
+                const int64_t off = (int64_t)base + incl - x;  // this lane's first pool slot
+                const bool fits = off + nleaf <= t.leaf_cap;
+                __syncwarp(FULL);  // the lanes' staged leaves, written this iteration, are read across lanes
+                // The warp writes the finished lanes' leaves together, leaf
+                // g of the warp's total going to lane g % 32, instead of each
+                // finished lane writing its own while the others wait: the
+                // owner of leaf g is the first lane whose inclusive count
+                // exceeds g (a five-step search over the counts).
+                for (int g0 = 0; g0 < total; g0 += 32) {
+                    const int gi = g0 + lane;
+                    int owner = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (__shfl_sync(FULL, incl, owner + step - 1) <= gi) owner += step;
+                    const int o_first = __shfl_sync(FULL, incl - x, owner);
+                    const bool o_fits = __shfl_sync(FULL, (int)fits, owner) != 0;
+                    const int64_t o_off = (int64_t)__shfl_sync(FULL, (unsigned long long)off, owner);
+                    const int i = gi - o_first;          // the leaf's index in its interval
+                    const int otid = (tid & ~31) + owner;  // the owner's staging column
+                    if constexpr (PREC == 1) {
+                        const float2* o_cff = reinterpret_cast<const float2*>(
+                            __shfl_sync(FULL, reinterpret_cast<unsigned long long>(cff), owner));
+                        const int o_code = CODE >= 0 ? CODE : __shfl_sync(FULL, code, owner);
+                        if (gi < total && o_fits) {
                             ff rl[MAX_COEF];
                             if constexpr (CODE >= 0)
-                                EvalFF<(CODE >= 0 ? CODE : 0)>::load(cff, rl);
+                                EvalFF<(CODE >= 0 ? CODE : 0)>::load(o_cff, rl);
                             else
-                                load_ff_dyn(code, cff, rl);
-                            for (int i = 0; i < nleaf; ++i) {
-                                const double vi = lf_v[i][tid];
-                                float q32;
-                                const float f32 = speed_slope32_of<CODE>(code, rl, (float)vi, q32);
-                                t.leaf_v[off + i] = vi;
-                                t.leaf_cum[off + i] = lf_c[i][tid];
-                                t.leaf_f[off + i] = f32;
-                                t.leaf_q[off + i] = q32;
-                            }
-                        } else {
-                            for (int i = 0; i < nleaf; ++i) {
-                                t.leaf_v[off + i] = lf_v[i][tid];
-                                t.leaf_cum[off + i] = lf_c[i][tid];
-                                t.leaf_f[off + i] = lf_f[i][tid];
-                                t.leaf_q[off + i] = lf_q[i][tid];
-                            }
+                                load_ff_dyn(o_code, o_cff, rl);
+                            const double vi = lf_v[i][otid];
+                            float q32;
+                            const float f32 = speed_slope32_of<CODE>(o_code, rl, (float)vi, q32);
+                            t.leaf_v[o_off + i] = vi;
+                            t.leaf_cum[o_off + i] = lf_c[i][otid];
+                            t.leaf_f[o_off + i] = f32;
+                            t.leaf_q[o_off + i] = q32;
                         }
                     } else {
+                        if (gi < total && o_fits) {
+                            t.leaf_v[o_off + i] = lf_v[i][otid];
+                            t.leaf_cum[o_off + i] = lf_c[i][otid];
+                            t.leaf_f[o_off + i] = lf_f[i][otid];
+                            t.leaf_q[o_off + i] = lf_q[i][otid];
+                        }
+                    }
+                }
+                if (fin) {
+                    if (!fits) {
                         // the pool is full: the deep passes redo this interval
                         const unsigned long long o = atomicAdd(t.ctr + C_DEEP, 1ull);
                         if ((int64_t)o < t.deep_cap)
