@@ -323,6 +323,7 @@ constexpr int STREAM_EVENTS = 4;  // host-buffer sampling: events per stage, use
 struct CodeRange {
     int code;
     int64_t begin, end;  // range of the grouped segment list
+    int64_t coef_base;   // coefficient index of the range's first segment
 };
 
 struct gcv_ctx {
@@ -635,21 +636,31 @@ gcv_status finish_create(gcv_ctx* c, const uint8_t* kind, const uint8_t* degree,
         std::vector<int64_t> base(64, 0);
         int64_t at = 0;
         c->code_ranges.clear();
+        int64_t coef_at = 0;
+        std::vector<int64_t> coef_base(64, 0);
         for (int cd = 0; cd < 64; ++cd) {
             base[(size_t)cd] = at;
+            coef_base[(size_t)cd] = coef_at;
             if (per_code[(size_t)cd] > 0) {
-                c->code_ranges.push_back(CodeRange{cd, at, at + per_code[(size_t)cd]});
+                c->code_ranges.push_back(CodeRange{cd, at, at + per_code[(size_t)cd], coef_at});
                 at += per_code[(size_t)cd];
+                coef_at += per_code[(size_t)cd] * code_stride(cd);
             }
         }
         if (c->code_ranges.size() > (size_t)(C_COUNT - C_WORK_CODE))
             return fail(GCV_ERR_INVALID, "too many distinct curve codes in one batch");
+        const std::vector<int64_t> range_begin = base;
         std::vector<int64_t> dst((size_t)n);
         for (int64_t i = 0; i < n; ++i) {
-            int64_t& nb = base[(size_t)code_of[(size_t)i]];
+            const int cd = code_of[(size_t)i];
+            int64_t& nb = base[(size_t)cd];
+            // the coefficient table follows the grouped list: curve i's
+            // first segment at its list position within the code's range
+            coef_off[(size_t)i] = coef_base[(size_t)cd] + (nb - range_begin[(size_t)cd]) * code_stride(cd);
             dst[(size_t)i] = nb;
             nb += seg_off[(size_t)i + 1] - seg_off[(size_t)i];
         }
+        CHECK(upload(c->coef_off, coef_off.data(), coef_off.size(), c->stream));
         // curves grouped the same way (sampling launches)
         std::vector<int64_t> curve_base(64, 0), per_code_curves(64, 0);
         for (int64_t i = 0; i < n; ++i) per_code_curves[(size_t)code_of[(size_t)i]]++;
@@ -842,19 +853,26 @@ gcv_status launch_main_pass(gcv_ctx* c, LengthParams P, bool capture = false)
         return GCV_OK;
     };
     for (bool& x : c->code_timed) x = false;
+    // work items in the order of the coefficient table and the learned
+    // start depths (segment order for one code, the grouped list otherwise)
+    P.by_item = 1;
     if (c->code >= 0) {
         P.list = nullptr;
         P.n_items = c->n_seg;
         P.work = c->ctr.p + C_WORK;
+        P.coef_base = 0;
         CHECK(mark(c->code, 0));
         CHECK(launch_length<0>(c, c->code, P));
         return mark(c->code, 1);
     }
+    const uint32_t* starts = P.starts;
     for (size_t k = 0; k < c->code_ranges.size(); ++k) {
         const CodeRange& r = c->code_ranges[k];
         if (r.end == r.begin) continue;
         P.list = c->seg_list.p + r.begin;
         P.n_items = r.end - r.begin;
+        P.coef_base = r.coef_base;
+        P.starts = starts ? starts + r.begin : nullptr;
         P.work = c->ctr.p + C_WORK_CODE + k;
         CHECK(mark(r.code, 0));
         CHECK(launch_length<0>(c, r.code, P));
@@ -1022,18 +1040,19 @@ gcv_status build_table(gcv_ctx* c)
         CHECK(c->starts.reserve((size_t)c->n_seg));
         CU(cudaMemsetAsync(c->starts.p, 0, (size_t)c->n_seg * sizeof(uint32_t), c->stream));
         const int md = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
-        auto run = [&](const uint4* f16, const int* list, int64_t n) -> gcv_status {
-            cudaError_t e = mlp_starts_launch_bf16(f16, list, n, c->mlp_w, md, c->starts.p, c->stream);
+        // start depths in the order of the work items (the grouped list)
+        auto run = [&](const uint4* f16, uint32_t* starts, int64_t n) -> gcv_status {
+            cudaError_t e = mlp_starts_launch_bf16(f16, nullptr, n, c->mlp_w, md, starts, c->stream);
             if (e != cudaSuccess) return cuda_fail(e, "network inference");
             c->stats.n_launches++;
             return GCV_OK;
         };
         if (c->code > 0) {
-            CHECK(run(c->feat16.p, nullptr, c->n_seg));
+            CHECK(run(c->feat16.p, c->starts.p, c->n_seg));
         } else if (c->code < 0) {
             for (const CodeRange& r : c->code_ranges)
                 if (r.code != CODE_ELLIPSE)
-                    CHECK(run(c->feat16.p + 2 * r.begin, c->seg_list.p + r.begin, r.end - r.begin));
+                    CHECK(run(c->feat16.p + 2 * r.begin, c->starts.p + r.begin, r.end - r.begin));
         }
     }
     CU(cudaEventRecord(c->ev[6], c->stream));
@@ -1373,17 +1392,18 @@ gcv_status enqueue_table_graph(gcv_ctx* c)
     if (learned) {
         CU(cudaMemsetAsync(c->starts.p, 0, (size_t)c->n_seg * sizeof(uint32_t), c->stream));
         const int md = mixed ? std::min(c->opt.max_depth, 44) : c->opt.max_depth;
-        auto run = [&](const uint4* f16, const int* list, int64_t n) -> gcv_status {
-            cudaError_t e = mlp_starts_launch_bf16(f16, list, n, c->mlp_w, md, c->starts.p, c->stream);
+        // start depths in the order of the work items (the grouped list)
+        auto run = [&](const uint4* f16, uint32_t* starts, int64_t n) -> gcv_status {
+            cudaError_t e = mlp_starts_launch_bf16(f16, nullptr, n, c->mlp_w, md, starts, c->stream);
             if (e != cudaSuccess) return cuda_fail(e, "network inference");
             return GCV_OK;
         };
         if (c->code > 0) {
-            CHECK(run(c->feat16.p, nullptr, c->n_seg));
+            CHECK(run(c->feat16.p, c->starts.p, c->n_seg));
         } else if (c->code < 0) {
             for (const CodeRange& r : c->code_ranges)
                 if (r.code != CODE_ELLIPSE)
-                    CHECK(run(c->feat16.p + 2 * r.begin, c->seg_list.p + r.begin, r.end - r.begin));
+                    CHECK(run(c->feat16.p + 2 * r.begin, c->starts.p + r.begin, r.end - r.begin));
         }
     }
     CU(cudaEventRecordWithFlags(c->ev[6], c->stream, cudaEventRecordExternal));

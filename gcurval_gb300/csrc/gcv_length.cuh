@@ -46,6 +46,13 @@ struct LengthParams {
     const float2* coef_ff;  // float-float copy of the coefficients (PREC 1)
     unsigned long long* work;  // work-queue head of this launch (starts at 0)
     const uint32_t* starts;    // learned quarter start depths per segment (NULL: plain walk)
+    // by_item (main pass of one curve code): the coefficients of work item i
+    // are at coef_base + i * code_stride(CODE) and its learned start depths
+    // at starts[i] (the table is laid out in the order of the grouped
+    // segment list), so a lane starts its interval's first panel without
+    // first loading the segment's curve and offsets
+    int by_item;
+    int64_t coef_base;
 };
 
 // Launches k_length<MODE, CODE, PREC> over P (persistent grid sized from the

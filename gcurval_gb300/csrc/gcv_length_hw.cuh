@@ -79,8 +79,12 @@ __global__ void __launch_bounds__(LK_THREADS) k_length_hw(LengthParams P)
                 exhausted = true;
             } else {
                 s = P.list ? (int64_t)P.list[item] : (int64_t)item;
-                const int64_t c = b.seg_curve[s];
-                cff = P.coef_ff + b.coef_off[c] + (s - b.seg_off[c]) * code_stride(CODE);
+                if (P.by_item) {
+                    cff = P.coef_ff + P.coef_base + (int64_t)item * code_stride(CODE);
+                } else {
+                    const int64_t c = b.seg_curve[s];
+                    cff = P.coef_ff + b.coef_off[c] + (s - b.seg_off[c]) * code_stride(CODE);
+                }
                 k = 0;
                 depth = 0;
                 nleaf = 0;
@@ -90,7 +94,7 @@ __global__ void __launch_bounds__(LK_THREADS) k_length_hw(LengthParams P)
                 dq = 0;
                 if constexpr (CODE > 0) {
                     if (P.starts) {
-                        const uint32_t q = P.starts[s];
+                        const uint32_t q = P.starts[P.by_item ? (int64_t)item : s];
                         ff rc[MAX_COEF];
                         EvalFF<CODE>::load(cff, rc);
                         const float ch = chord_of<CODE>(rc);

@@ -151,9 +151,17 @@ __global__ void __launch_bounds__(LK_THREADS, (MODE == 0 && PREC == 1) ? length_
                     exhausted = true;
                 } else {
                     s = P.list ? (int64_t)P.list[item] : item;
-                    const int64_t c = b.seg_curve[s];
-                    if (CODE < 0) code = curve_code(b, c);
-                    const int64_t ci = b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
+                    // the main pass of one code addresses the table by work
+                    // item (no dependent loads before the first panel)
+                    const bool by_item = MODE == 0 && CODE >= 0 && P.by_item;
+                    int64_t ci;
+                    if (by_item) {
+                        ci = P.coef_base + item * code_stride(code);
+                    } else {
+                        const int64_t c = b.seg_curve[s];
+                        if (CODE < 0) code = curve_code(b, c);
+                        ci = b.coef_off[c] + (s - b.seg_off[c]) * code_stride(code);
+                    }
                     if constexpr (PREC == 1) {
                         cff = P.coef_ff + ci;
                     } else {
@@ -172,7 +180,7 @@ __global__ void __launch_bounds__(LK_THREADS, (MODE == 0 && PREC == 1) ? length_
                     if constexpr (MODE == 0 && CODE > 0) {
                         // learned start: the predicted depths, tolerance from the chord
                         if (P.starts) {
-                            const uint32_t q = P.starts[s];
+                            const uint32_t q = P.starts[by_item ? item : s];
                             float ch;
                             if constexpr (PREC == 1) {
                                 ff rc[MAX_COEF];
@@ -196,7 +204,10 @@ __global__ void __launch_bounds__(LK_THREADS, (MODE == 0 && PREC == 1) ? length_
                             pool = -1;
                         }
                     }
-                    if (t.seg_t1[s] == t.seg_t0[s]) {  // zero-width knot interval: one empty leaf
+                    // zero-width knot interval: one empty leaf (the main pass
+                    // by work item walks it: its coefficients are zero, so the
+                    // root panel is accepted with length 0 and the same leaf)
+                    if (!by_item && t.seg_t1[s] == t.seg_t0[s]) {
                         if (MODE == 0) {
                             lf_v[0][tid] = 1.0;
                             lf_c[0][tid] = 0.0;
