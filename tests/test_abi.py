@@ -104,3 +104,40 @@ def test_bundle_and_f32_arguments_rejected_without_gpu():
                                        ctypes.byref(o)) == _lib.GCV_ERR_INVALID
     assert lib.gcv_create_ellipses_f32(ctypes.byref(h), -1, None, None, None, None, None, _lib.GCV_HOST,
                                        ctypes.byref(o)) == _lib.GCV_ERR_INVALID
+
+
+def _c_struct_fields(header_text: str, name: str):
+    """Field names of `typedef struct name { ... } name;` in the public header."""
+    body = re.search(r"typedef struct " + name + r" \{(.*?)\} " + name + ";", header_text, re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for decl in body.split(";"):
+        decl = decl.strip()
+        if not decl:
+            continue
+        # "type a, b[N], c": the first declarator carries the type
+        for part in decl.split(","):
+            fields.append(re.findall(r"([A-Za-z_][A-Za-z0-9_]*)\s*(?:\[[^\]]*\])?\s*$", part.strip())[0])
+    return fields
+
+
+def test_ctypes_structs_mirror_the_header():
+    # the Python binding passes these structs by pointer: their fields must be
+    # the header's, in the header's order
+    text = open(_lib.HEADER).read()
+    for py, cname in ((_lib.Options, "gcv_options"), (_lib.Result, "gcv_result"), (_lib.Stats, "gcv_stats")):
+        c_fields = _c_struct_fields(text, cname)
+        py_fields = [f[0] for f in py._fields_]
+        assert py_fields == c_fields, cname
+
+
+def test_page_locked_allocation_needs_a_gpu():
+    # the helpers for page-locked host arrays fail loudly without a device
+    lib = g.load()
+    if lib.gcv_measure_fma_peak(0, ctypes.byref(ctypes.c_double())) == _lib.GCV_OK:
+        pytest.skip("a GPU is present")
+    with pytest.raises(g.GcvError):
+        g.pinned_empty(16)
+    p = ctypes.c_void_p()
+    assert lib.gcv_host_alloc(0, ctypes.byref(p)) == _lib.GCV_OK and not p.value
+    assert lib.gcv_host_free(None) == _lib.GCV_OK
