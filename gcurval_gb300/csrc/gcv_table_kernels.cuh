@@ -130,7 +130,7 @@ static __global__ void k_deep_total(const int* __restrict__ list, int64_t n, con
 // replacing the reference's per-segment Brent-Kung scan plus one thread per
 // curve doing a sequential Kahan sum (gcurval/detail/cuda/kernel/generic.inl.cuh:52-137).
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_ITEMS = 32;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 constexpr long long SCAN_SPIN_LIMIT = 1ll << 22;
 
@@ -165,9 +165,12 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, 
     if (tile >= n_tiles) return;
     const int64_t base = tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
 
-    // Within a thread: plain FP64 running sums of at most SCAN_ITEMS lengths
-    // since the last curve start (rounding <= 16 ulp of the partial sum);
-    // across threads, tiles and the look-back: double-double.
+    // Within a warp: plain FP64 running sums of at most SCAN_ITEMS lengths
+    // since the last curve start per thread, and a plain FP64 scan of the 32
+    // thread sums (at most 1,024 lengths, rounding <= 37 ulp of the partial
+    // sum); across warps, tiles and the look-back, where the sums grow long:
+    // double-double.  The FP64 pipe bounds this kernel, and the warp-level
+    // double-double carries were most of its FP64 operations.
     double part[SCAN_ITEMS];  // running sum since the last start within the thread
     unsigned heads = 0;       // bit k: item k starts a curve
     int prev_curve = base > 0 && base - 1 < b.n_seg ? b.seg_curve[base - 1] : -1;
@@ -185,16 +188,19 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, 
         run = (heads >> k) & 1u ? x : run + x;
         part[k] = run;
     }
-    // thread aggregate
-    const SegVal agg{heads != 0, DD{run, 0.0}};
-    // warp inclusive scan of aggregates
-    SegVal inc = agg;
+    // warp inclusive scan of the thread aggregates (seg_combine in FP64)
+    int inc_flag = heads != 0;
+    double inc_v = run;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-        const SegVal y = shfl_up_sv(inc, d);
-        if (lane >= d) inc = seg_combine(y, inc);
+        const int yf = __shfl_up_sync(0xffffffffu, inc_flag, d);
+        const double yv = __shfl_up_sync(0xffffffffu, inc_v, d);
+        if (lane >= d && !inc_flag) {
+            inc_v = yv + inc_v;
+            inc_flag = yf;
+        }
     }
-    if (lane == 31) s_warp[warp] = inc;
+    if (lane == 31) s_warp[warp] = SegVal{inc_flag, DD{inc_v, 0.0}};
     __syncthreads();
     if (warp == 0) {
         SegVal w = lane < SCAN_THREADS / 32 ? s_warp[lane] : SegVal{0, DD{0.0, 0.0}};
@@ -207,8 +213,9 @@ static __global__ void __launch_bounds__(SCAN_THREADS) k_scan(Batch b, Table t, 
     }
     __syncthreads();
     // exclusive prefix of this thread inside the tile
-    SegVal excl = shfl_up_sv(inc, 1);
-    if (lane == 0) excl = SegVal{0, DD{0.0, 0.0}};
+    const int ex_flag = __shfl_up_sync(0xffffffffu, inc_flag, 1);
+    const double ex_v = __shfl_up_sync(0xffffffffu, inc_v, 1);
+    SegVal excl = lane == 0 ? SegVal{0, DD{0.0, 0.0}} : SegVal{ex_flag, DD{ex_v, 0.0}};
     if (warp > 0) excl = lane == 0 ? s_warp[warp - 1] : seg_combine(s_warp[warp - 1], excl);
 
     // decoupled look-back by thread 0
